@@ -1,0 +1,286 @@
+/*
+ * sf_align.h -- C ABI of the GB300 (sm_103a) alignment stage for spearfish.
+ *
+ * Drop-in for the alignment entry points of spearfish's `map::align`
+ * (crates/map/src/align.rs, v0.3.2).  Each function below names the
+ * reference item it replaces.  All computation runs on the GPU; there is no
+ * CPU fallback: without a usable CUDA device every call fails with
+ * SF_ERR_CUDA.
+ *
+ * Conventions
+ *  - Sequences are byte codes, one base per byte, exactly as the reference's
+ *    `&[u8]` inputs: 0..3 = A, C, G, T.  Myers and the affine passes use
+ *    `code & 3` (align.rs:78,120,2557); the local band's read may hold codes
+ *    of 4 or more, which match nothing (align.rs:731-734).
+ *  - `usize::MAX` arguments (no band, no cut) are SF_NOLIMIT.
+ *  - Myers' `Option<u32>` is a uint32_t with SF_NONE for `None`.
+ *  - Scores that the reference reports as unreachable are SF_NEG
+ *    (align.rs:693, `i32::MIN / 4`).
+ *  - Every function returns SF_OK (0) or a negative SF_ERR_* code;
+ *    sf_last_error() gives a message for the calling thread.
+ *  - Threading: any thread may call any function.  The one-call entry points
+ *    use a per-thread context (its own CUDA stream and buffers) on the
+ *    current device, as the reference keeps per-thread DP buffers
+ *    (align.rs:2167-2171).  Explicit contexts (sf_context_*) are for the
+ *    batched and serving forms; one context must not be used by two threads
+ *    at once.
+ */
+#ifndef SF_ALIGN_H
+#define SF_ALIGN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SF_OK 0
+#define SF_ERR_INVALID (-1)  /* bad argument */
+#define SF_ERR_CUDA (-2)     /* no device / CUDA runtime error */
+#define SF_ERR_NOMEM (-3)    /* device or pinned allocation failed */
+#define SF_ERR_TOO_LONG (-4) /* a sequence exceeds the supported length */
+#define SF_ERR_TIMEOUT (-5)  /* a bounded wait ran out */
+#define SF_ERR_CAPACITY (-6) /* an output buffer is too small */
+#define SF_ERR_BUSY (-7)     /* serving: no slot or memory free */
+
+#define SF_NONE UINT32_MAX
+#define SF_NOLIMIT UINT64_MAX
+#define SF_NEG (INT32_MIN / 4)
+
+/* Longest pattern (read segment) the Myers kernels take, in bases. */
+#define SF_MYERS_MAX_PATTERN 32768u
+
+/* align.rs:40-45 `Mode`. */
+typedef enum { SF_INFIX = 0, SF_PREFIX = 1, SF_GLOBAL = 2 } sf_mode;
+
+/* align.rs:660-668 `Affine`: +mat per match, -mis per mismatch,
+ * -(open + ext * l) per gap of length l. */
+typedef struct {
+    int32_t mat, mis, open, ext;
+} sf_affine_t;
+
+/* align.rs:678-690 `Affine::ONT`, `Affine::HIFI`. */
+#define SF_AFFINE_ONT ((sf_affine_t){2, 4, 4, 2})
+#define SF_AFFINE_HIFI ((sf_affine_t){1, 4, 6, 2})
+
+/* ---- errors and devices ------------------------------------------------ */
+
+const char *sf_last_error(void);
+/* Library and kernel build identification (static string). */
+const char *sf_version(void);
+/* Selects the device the calling thread's one-call context uses
+ * (default: the CUDA current device when the thread first calls in). */
+int sf_set_device(int device);
+
+/* ---- drop-in entry points (map::align) ---------------------------------- */
+
+/* align.rs:88-91 `distance` (and `distance_with`, align.rs:93-168). */
+int sf_distance(const uint8_t *pattern, uint64_t m, const uint8_t *text,
+                uint64_t n, int mode, uint32_t k, uint32_t *out);
+
+/* align.rs:174-200 `batch_distances`: one pattern, `count` texts, one k.
+ * texts[q] points at lens[q] codes. */
+int sf_batch_distances(const uint8_t *pattern, uint64_t m,
+                       const uint8_t *const *texts, const uint64_t *lens,
+                       uint64_t count, int mode, uint32_t k, uint32_t *out);
+
+/* align.rs:655-658 `infix_distance`. */
+int sf_infix_distance(const uint8_t *pattern, uint64_t m, const uint8_t *text,
+                      uint64_t n, uint32_t *out);
+
+/* align.rs:699-701 `affine`. band = SF_NOLIMIT for the exact score. */
+int sf_affine(const uint8_t *pattern, uint64_t m, const uint8_t *text,
+              uint64_t n, int mode, const sf_affine_t *sc, uint64_t band,
+              int32_t *out);
+
+/* align.rs:710-729 `affine_extend`. xdrop = INT32_MAX for none. */
+int sf_affine_extend(const uint8_t *pattern, uint64_t m, const uint8_t *text,
+                     uint64_t n, const sf_affine_t *sc, uint64_t band,
+                     int32_t end_bonus, int32_t xdrop, int32_t *out);
+
+/* align.rs:951-982 `affine_extend_window` result: (score, pattern bases,
+ * text bases, text bases read). */
+typedef struct {
+    int32_t score;
+    int32_t pad_;
+    uint64_t pattern_bases;
+    uint64_t text_bases;
+    uint64_t text_read;
+} sf_extend_t;
+
+int sf_affine_extend_window(const uint8_t *pattern, uint64_t m,
+                            const uint8_t *text, uint64_t n, uint64_t window,
+                            const sf_affine_t *sc, uint64_t band,
+                            int32_t end_bonus, int32_t xdrop, sf_extend_t *out);
+
+/* align.rs:854-861 `affine_sorted`: results equal one `affine` per text. */
+int sf_affine_sorted(const uint8_t *pattern, uint64_t m,
+                     const uint8_t *const *texts, const uint64_t *lens,
+                     uint64_t count, int mode, const sf_affine_t *sc,
+                     uint64_t band, int32_t *out);
+
+/* align.rs:863-901 `affine_extend_sorted_cut` result per text:
+ * (whole text, text cut at `cut`, text bases covered). */
+typedef struct {
+    int32_t whole;
+    int32_t cut;
+    uint64_t cols;
+} sf_cut_t;
+
+/* align.rs:880-901 `affine_extend_sorted_cut`. */
+int sf_affine_extend_sorted_cut(const uint8_t *pattern, uint64_t m,
+                                const uint8_t *const *texts,
+                                const uint64_t *lens, uint64_t count,
+                                const sf_affine_t *sc, uint64_t band,
+                                int32_t end_bonus, int32_t xdrop, int diagonal,
+                                uint64_t window, uint64_t cut, sf_cut_t *out);
+
+/* align.rs:903-949 `affine_extend_sorted_cut_bonus`. */
+int sf_affine_extend_sorted_cut_bonus(
+    const uint8_t *pattern, uint64_t m, const uint8_t *const *texts,
+    const uint64_t *lens, uint64_t count, const sf_affine_t *sc, uint64_t band,
+    int32_t end_bonus, int32_t xdrop, int diagonal, uint64_t window,
+    uint64_t cut, int track_cut, int bonus_within_cut, sf_cut_t *out);
+
+/* align.rs:731-737 `local_band`. */
+int sf_local_band(const uint8_t *read, uint64_t m, const uint8_t *text,
+                  uint64_t n, const sf_affine_t *sc, int64_t dlo, int64_t dhi,
+                  int32_t end_bonus, int32_t *out);
+
+/* align.rs:741-760 `local_band_ends`. */
+int sf_local_band_ends(const uint8_t *read, uint64_t m, const uint8_t *text,
+                       uint64_t n, const sf_affine_t *sc, int64_t dlo,
+                       int64_t dhi, int32_t bonus_start, int32_t bonus_end,
+                       int32_t *out);
+
+/* align.rs:2172-2176 `dp_work`: banded-affine cells and rows computed by the
+ * calling thread's passes so far (counted always; the reference counts them
+ * only with SPEARFISH_STATS). */
+void sf_dp_work(uint64_t *cells, uint64_t *rows);
+
+/* ---- traceback / CIGAR (new: the reference has no traceback) ------------
+ * ops are BAM-style words (len << 4 | op), op 0 = M, 1 = I (pattern base
+ * against no text base), 2 = D (text base against no pattern base),
+ * 4 = S (pattern bases past the extension's end cell).  Tie order: H from
+ * H' (diagonal or vertical) before E; diagonal before vertical; gap opening
+ * before extending.  The CIGAR re-scores to `score` (minus the end bonus
+ * where `score` includes it). */
+typedef struct {
+    int32_t score;    /* the entry point's score */
+    int32_t status;   /* 0 ok, 1 no path (unreachable end), -1 capacity */
+    uint64_t pattern_end; /* pattern bases the path covers (ends there) */
+    uint64_t text_start;  /* text column the path starts at (Infix) */
+    uint64_t text_end;    /* text column the path ends at */
+    uint64_t n_ops;
+} sf_cigar_t;
+
+/* `affine` with the path of its best cell. */
+int sf_affine_cigar(const uint8_t *pattern, uint64_t m, const uint8_t *text,
+                    uint64_t n, int mode, const sf_affine_t *sc, uint64_t band,
+                    uint32_t *ops, uint64_t cap, sf_cigar_t *out);
+
+/* `affine_extend_window` with the path of the extension. */
+int sf_affine_extend_window_cigar(const uint8_t *pattern, uint64_t m,
+                                  const uint8_t *text, uint64_t n,
+                                  uint64_t window, const sf_affine_t *sc,
+                                  uint64_t band, int32_t end_bonus,
+                                  int32_t xdrop, uint32_t *ops, uint64_t cap,
+                                  sf_cigar_t *out);
+
+/* ---- batched form --------------------------------------------------------
+ * Thousands of (pattern, text) jobs of uneven length in one length-bucketed,
+ * persistent launch per bucket, captured in a CUDA graph.  Sequences live in
+ * one caller pool of byte codes; each job names its pattern and text by byte
+ * offset and length. */
+
+typedef struct sf_context sf_context;
+
+int sf_context_create(int device, sf_context **out);
+void sf_context_destroy(sf_context *ctx);
+
+enum {
+    SF_JOB_MYERS = 0,         /* `distance` in `mode` with threshold k */
+    SF_JOB_AFFINE = 1,        /* `affine` in `mode` (score, optional CIGAR) */
+    SF_JOB_EXTEND_WINDOW = 2, /* `affine_extend_window` (optional CIGAR) */
+    SF_JOB_LOCAL = 3          /* `local_band_ends` */
+};
+
+typedef struct {
+    uint64_t p_off; /* pattern: byte offset in the pool */
+    uint64_t t_off; /* text: byte offset in the pool */
+    uint32_t m, n;  /* lengths */
+    uint8_t kind;   /* SF_JOB_* */
+    uint8_t mode;   /* sf_mode (Myers, affine) */
+    uint8_t want_cigar;
+    uint8_t pad_;
+    uint32_t k;      /* Myers threshold (SF_NONE: none) */
+    uint64_t band;   /* affine band (SF_NOLIMIT: none) */
+    uint64_t window; /* extend window */
+    int64_t dlo, dhi; /* local band diagonals */
+    int32_t end_bonus, end_bonus2; /* extend bonus; local (start, end) */
+    int32_t xdrop;
+    uint32_t sc_index; /* index into the batch's scoring table */
+} sf_job_t;
+
+typedef struct {
+    int32_t score;      /* affine / extend / local score */
+    uint32_t distance;  /* Myers: SF_NONE for None */
+    uint64_t pattern_end, text_start, text_end, text_read;
+    uint64_t cells;     /* DP cells computed (GCUPS numerator) */
+    uint64_t cigar_off; /* first op of this job's CIGAR in the op pool */
+    uint32_t n_ops;
+    int32_t status;     /* 0 ok; 1 no path; negative SF_ERR_* */
+} sf_result_t;
+
+/* A batch prepared once and run many times: descriptors, bucketing and
+ * device buffers are built at creation; sf_plan_execute launches the bucket
+ * kernels (captured into a CUDA graph on first use) on inputs already
+ * resident in HBM. */
+typedef struct sf_plan sf_plan;
+
+int sf_plan_create(sf_context *ctx, const sf_job_t *jobs, uint64_t count,
+                   const sf_affine_t *scores, uint32_t n_scores,
+                   uint64_t pool_bytes, sf_plan **out);
+void sf_plan_destroy(sf_plan *plan);
+/* Host pool -> device (pinned staging, async on the plan's stream). */
+int sf_plan_upload(sf_plan *plan, const uint8_t *pool);
+/* Run every job on the resident inputs (asynchronous). */
+int sf_plan_execute(sf_plan *plan);
+/* Results (and compacted CIGAR ops) -> host; waits for the plan's stream.
+ * ops may be NULL when no job wants a CIGAR. */
+int sf_plan_download(sf_plan *plan, sf_result_t *results, uint32_t *ops,
+                     uint64_t ops_cap, uint64_t *ops_used);
+/* Blocks until the plan's work is done. */
+int sf_plan_sync(sf_plan *plan);
+/* The plan's CUDA stream (cudaStream_t) for event timing. */
+void *sf_plan_stream(sf_plan *plan);
+/* Kernel launches one execute issues (for launch accounting). */
+uint64_t sf_plan_launches(const sf_plan *plan);
+/* Description of the plan's buckets as a static-lifetime JSON string. */
+const char *sf_plan_describe(sf_plan *plan);
+
+/* Runs one execute in order on the plan's stream with CUDA events between
+ * its stages -- pack, each bucket (in sf_plan_describe's order), then the
+ * traceback walk with CIGAR compaction -- and returns each stage's ms. */
+int sf_plan_profile(sf_plan *plan, float *ms, uint32_t cap,
+                    uint32_t *n_stages);
+
+/* One call on the context's reusable plan: descriptors, upload, execute,
+ * download (buffers grow and are reused across calls). */
+int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
+                 const sf_job_t *jobs, uint64_t count,
+                 const sf_affine_t *scores, uint32_t n_scores,
+                 sf_result_t *results, uint32_t *ops, uint64_t ops_cap,
+                 uint64_t *ops_used);
+
+/* ---- diagnostics -------------------------------------------------------- */
+
+/* Measured int32 throughput of `device` (tera-ops/s) on the DP kernels'
+ * add-then-max instruction mix: the roofline of the integer-bound DP. */
+int sf_int_peak(int device, double *tops, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,9 @@
+// Register-row banded affine kernels with C = 4 cells per lane (bands up to 128 cells).
+#include "sf_affine_impl.cuh"
+
+namespace sfk {
+cudaError_t launch_affine_regs_4(bool tb, const AffLaunch& a, int grid, int block,
+                                  cudaStream_t s) {
+  return launch_affine_c<4, false>(tb, a, grid, block, s);
+}
+}  // namespace sfk

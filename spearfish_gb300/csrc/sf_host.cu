@@ -1,0 +1,1396 @@
+// Host side of the C ABI (include/sf_align.h): device contexts, batch plans (length
+// bucketing, HBM layout, persistent launches captured in a CUDA graph) and the one-call
+// entry points that mirror crates/map/src/align.rs.
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/sf_align.h"
+#include "sf_internal.cuh"
+
+namespace {
+
+using namespace sf;
+
+thread_local std::string g_err;
+thread_local uint64_t g_dp_cells = 0, g_dp_rows = 0;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(e_ == cudaErrorMemoryAllocation ? SF_ERR_NOMEM : SF_ERR_CUDA,     \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
+  } while (0)
+
+inline uint64_t usat_add(uint64_t a, uint64_t b) { return a > UINT64_MAX - b ? UINT64_MAX : a + b; }
+inline uint64_t usat_sub(uint64_t a, uint64_t b) { return a > b ? a - b : 0; }
+inline int32_t sat_add32(int32_t a, int32_t b) {
+  int64_t s = (int64_t)a + b;
+  return s > INT32_MAX ? INT32_MAX : s < INT32_MIN ? INT32_MIN : (int32_t)s;
+}
+constexpr int64_t kGeoCap = int64_t(1) << 40;  // band geometry beyond any text length
+
+// ---- device and pinned buffers ---------------------------------------------------------
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int ensure(size_t n) {
+    if (n <= cap) return SF_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      return fail(SF_ERR_NOMEM, "cudaMalloc(" + std::to_string(want) + "): " + cudaGetErrorString(e));
+    }
+    cap = want;
+    return SF_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct PinBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~PinBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  int ensure(size_t n) {
+    if (n <= cap) return SF_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 256;
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      return fail(SF_ERR_NOMEM, "cudaMallocHost: " + std::string(cudaGetErrorString(e)));
+    }
+    cap = want;
+    return SF_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+}  // namespace
+
+namespace {
+
+// ---- passes ----------------------------------------------------------------------------
+
+enum PassKind : uint8_t { PK_MYERS = 0, PK_AFFINE = 1, PK_LOCAL = 2 };
+
+// One DP pass as the reference's `affine_dp` / `distance` / `local_band_core` receive it.
+struct Pass {
+  PassKind kind;
+  uint8_t mode = 0;
+  bool clip = false, cell = false, want_cigar = false;
+  uint8_t tb_kind = 0;  // 0: affine end, 1: extend-window end
+  uint64_t p_off = 0, t_off = 0;  // byte offsets in the pool
+  uint32_t m = 0, n = 0;
+  uint64_t band = SF_NOLIMIT, geom = 0, cut = SF_NOLIMIT;
+  int32_t xdrop = 0, end_bonus = 0, bonus0 = 0, bonus1 = 0;
+  int64_t dlo = 0, dhi = 0;
+  uint32_t k = SF_NONE;
+  sf_affine_t sc{2, 4, 4, 2};
+};
+
+struct Bucket {
+  PassKind kind;
+  int c = 0;       // affine: cells per lane; Myers: blocks per lane
+  bool wide = false, tb = false;
+  int lanes = 32;  // Myers: lanes per pair
+  uint32_t first = 0, count = 0;  // range in the order array
+  int grid = 0, block = 128;
+  uint64_t scratch_off = 0;       // wide rows: this bucket's slice of the scratch (int32s)
+};
+
+}  // namespace
+
+struct sf_plan {
+  sf_context* ctx = nullptr;
+  bool owns_ctx = false;
+  std::vector<Pass> passes;
+  // Sequences: unique (byte offset, length), packed word offsets.
+  std::vector<uint64_t> seq_boff, seq_woff;
+  std::vector<uint32_t> seq_len;
+  uint64_t pool_bytes = 0, pool_words = 0;
+  // Per pass: index in its kind's device arrays.
+  std::vector<uint32_t> slot;
+  uint32_t n_aff = 0, n_my = 0, n_walk = 0;
+  std::vector<Bucket> buckets;
+  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
+  int wide_warps = 0;
+  std::string desc;
+  // Device buffers.
+  DevBuf d_bytes, d_pool, d_seq, d_djobs, d_params, d_res, d_mjobs, d_mout, d_tjobs, d_tres,
+      d_tb, d_ops, d_opsc, d_offs, d_order, d_counters, d_wlist, d_cls, d_scratch, d_total;
+  // Pinned staging.
+  PinBuf h_stage, h_res, h_mout, h_tres, h_ops;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_tried = false;
+  uint64_t launches = 0;
+  ~sf_plan() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (owns_ctx) delete ctx;
+  }
+};
+
+// ---- context ---------------------------------------------------------------------------
+
+struct sf_context {
+  int dev = 0;
+  int sms = 0;
+  cudaStream_t s = nullptr;
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork = nullptr, join[kAux] = {};
+  std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
+  ~sf_context() {
+    cache.reset();
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(dev);
+    for (int i = 0; i < kAux; ++i) {
+      if (aux[i]) cudaStreamDestroy(aux[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (s) cudaStreamDestroy(s);
+    cudaSetDevice(prev);
+  }
+};
+
+namespace {
+
+int make_context(int device, sf_context** out) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    (void)cudaGetLastError();
+    return fail(SF_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= n) return fail(SF_ERR_INVALID, "device index out of range");
+  std::unique_ptr<sf_context> c(new sf_context);
+  c->dev = device;
+  CK(cudaSetDevice(device));
+  CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device));
+  CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+  for (int i = 0; i < sf_context::kAux; ++i) {
+    CK(cudaStreamCreateWithFlags(&c->aux[i], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->join[i], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+  *out = c.release();
+  return SF_OK;
+}
+
+int choose_affine_class(int64_t wmax, int& c, bool& wide) {
+  for (int q = 0; q < sfk::kAffineNC; ++q)
+    if (32 * (int64_t)sfk::kAffineC[q] >= wmax) {
+      c = sfk::kAffineC[q];
+      wide = false;
+      return SF_OK;
+    }
+  c = sfk::kWideC;
+  wide = true;
+  return SF_OK;
+}
+
+int choose_myers_class(uint32_t m, int& b, int& lanes) {
+  const uint32_t blocks = (m + 63) / 64;
+  if (m > SF_MYERS_MAX_PATTERN) return fail(SF_ERR_TOO_LONG, "Myers pattern longer than SF_MYERS_MAX_PATTERN");
+  if (blocks <= 32) {
+    b = 1;
+    lanes = 1;
+    while ((uint32_t)lanes < blocks) lanes <<= 1;
+    return SF_OK;
+  }
+  lanes = 32;
+  for (int q = 0; q < sfk::kMyersNB; ++q)
+    if (32u * (uint32_t)sfk::kMyersB[q] >= blocks) {
+      b = sfk::kMyersB[q];
+      return SF_OK;
+    }
+  return fail(SF_ERR_TOO_LONG, "pattern too long for the Myers kernels");
+}
+
+DJob make_djob(const Pass& p, const sf_plan& P, uint32_t& flags) {
+  DJob j{};
+  j.m = p.m;
+  j.n = p.n;
+  flags = 0;
+  if (p.kind == PK_LOCAL) {
+    flags = F_LOCAL | F_ROWMAX;
+    j.below = std::max<int64_t>(std::min<int64_t>(p.dlo, kGeoCap), -kGeoCap);
+    j.above = std::max<int64_t>(std::min<int64_t>(p.dhi, kGeoCap), -kGeoCap);
+  } else {
+    flags = p.mode & 3u;
+    const bool full = p.mode == SF_INFIX || p.band == SF_NOLIMIT;
+    if (full) flags |= F_FULL;
+    const uint64_t below = usat_add(p.band, usat_sub(p.m, p.geom));
+    const uint64_t above = usat_add(p.band, usat_sub(p.geom, p.m));
+    j.below = (int64_t)std::min<uint64_t>(below, (uint64_t)kGeoCap);
+    j.above = (int64_t)std::min<uint64_t>(above, (uint64_t)kGeoCap);
+    if (p.clip) flags |= F_CLIP | F_ROWMAX;
+    if (p.clip && p.cell) flags |= F_CELL;
+    if (p.cut != SF_NOLIMIT) flags |= F_CUT | F_ROWMAX;
+    j.cut = p.cut;
+  }
+  (void)P;
+  return j;
+}
+
+uint64_t seq_words(uint64_t len) { return (len + 1 + 15) / 16; }
+
+// Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
+int plan_build(sf_plan* P) {
+  sf_context* ctx = P->ctx;
+  CK(cudaSetDevice(ctx->dev));
+  const size_t np = P->passes.size();
+  if (np > 0xffffffffull / 2) return fail(SF_ERR_INVALID, "too many jobs");
+  // Unique sequences.
+  struct Key {
+    uint64_t off;
+    uint32_t len;
+    uint32_t idx;
+  };
+  std::vector<Key> keys;
+  keys.reserve(2 * np);
+  for (size_t q = 0; q < np; ++q) {
+    const Pass& p = P->passes[q];
+    if (p.p_off + p.m > P->pool_bytes || p.t_off + p.n > P->pool_bytes)
+      return fail(SF_ERR_INVALID, "job sequence outside the pool");
+    keys.push_back({p.p_off, p.m, (uint32_t)(2 * q)});
+    keys.push_back({p.t_off, p.n, (uint32_t)(2 * q + 1)});
+  }
+  std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+    return a.off != b.off ? a.off < b.off : a.len < b.len;
+  });
+  std::vector<uint64_t> word_of(2 * np);
+  P->seq_boff.clear();
+  P->seq_len.clear();
+  P->seq_woff.clear();
+  uint64_t words = 0;
+  for (size_t q = 0; q < keys.size(); ++q) {
+    if (q == 0 || keys[q].off != keys[q - 1].off || keys[q].len != keys[q - 1].len) {
+      P->seq_boff.push_back(keys[q].off);
+      P->seq_len.push_back(keys[q].len);
+      P->seq_woff.push_back(words);
+      words += seq_words(keys[q].len);
+    }
+    word_of[keys[q].idx] = P->seq_woff.back();
+  }
+  P->pool_words = words + 256;  // slack: kernels read whole windows past a sequence's end
+
+  // Per-kind arrays.
+  std::vector<DJob> dj;
+  std::vector<DParams> dp;
+  std::vector<TJob> tj;
+  std::vector<uint8_t> cls;
+  std::vector<MJob> mj;
+  std::vector<uint32_t> wlist;
+  P->slot.assign(np, 0);
+  struct Item {
+    uint32_t slot;
+    uint64_t work;
+  };
+  struct Key2 {
+    int kind, c, wide, tb, lanes;
+    bool operator<(const Key2& o) const {
+      return std::tie(kind, c, wide, tb, lanes) < std::tie(o.kind, o.c, o.wide, o.tb, o.lanes);
+    }
+    bool operator==(const Key2& o) const {
+      return kind == o.kind && c == o.c && wide == o.wide && tb == o.tb && lanes == o.lanes;
+    }
+  };
+  std::vector<std::pair<Key2, Item>> items;
+  items.reserve(np);
+  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
+  for (size_t q = 0; q < np; ++q) {
+    const Pass& p = P->passes[q];
+    if (p.kind == PK_MYERS) {
+      int b = 1, lanes = 1;
+      int rc = choose_myers_class(p.m, b, lanes);
+      if (rc) return rc;
+      MJob m{};
+      m.p_word = word_of[2 * q];
+      m.t_word = word_of[2 * q + 1];
+      m.m = p.m;
+      m.n = p.n;
+      m.mode = p.mode;
+      m.k = p.k;
+      P->slot[q] = (uint32_t)mj.size();
+      items.push_back({Key2{PK_MYERS, b, 0, 0, lanes}, Item{(uint32_t)mj.size(), (uint64_t)p.n}});
+      mj.push_back(m);
+      continue;
+    }
+    uint32_t flags = 0;
+    DJob j = make_djob(p, *P, flags);
+    j.p_word = word_of[2 * q];
+    j.t_word = word_of[2 * q + 1];
+    j.p_byte = p.p_off;
+    const int64_t wmax = band_wmax(j, flags);
+    int c = 4;
+    bool wide = false;
+    choose_affine_class(wmax, c, wide);
+    const bool tb = p.want_cigar && p.kind != PK_LOCAL;
+    if (tb) {
+      flags |= F_TB;
+      j.tb_word = tb_words;
+      const int64_t chunks = wide ? wide_chunks(c, wmax) : 1;
+      tb_words += (uint64_t)p.m * tb_row_words(c, chunks);
+    }
+    if (wide) scratch_cells = std::max<uint64_t>(scratch_cells, (uint64_t)wide_chunks(c, wmax) * 32 * c);
+    DParams pr{};
+    pr.flags = flags;
+    pr.xdrop = p.xdrop;
+    pr.bonus0 = p.bonus0;
+    pr.bonus1 = p.bonus1;
+    pr.mat = p.sc.mat;
+    pr.mis = p.sc.mis;
+    pr.open = p.sc.open;
+    pr.ext = p.sc.ext;
+    TJob t{};
+    if (tb) {
+      t.ops_off = ops_words;
+      const uint64_t cap = (uint64_t)p.m + p.n + 2;
+      t.ops_cap = (uint32_t)std::min<uint64_t>(cap, 0xffffffffull);
+      ops_words += cap;
+      t.kind = p.tb_kind;
+      t.end_bonus = p.end_bonus;
+      wlist.push_back((uint32_t)dj.size());
+    }
+    P->slot[q] = (uint32_t)dj.size();
+    const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
+    items.push_back({Key2{p.kind == PK_LOCAL ? PK_AFFINE : PK_AFFINE, c, wide, tb, 32},
+                     Item{(uint32_t)dj.size(), work}});
+    dj.push_back(j);
+    dp.push_back(pr);
+    tj.push_back(t);
+    cls.push_back((uint8_t)(wide ? (0x80 | c) : c));
+  }
+  P->n_aff = (uint32_t)dj.size();
+  P->n_my = (uint32_t)mj.size();
+  P->n_walk = (uint32_t)wlist.size();
+  P->tb_words = tb_words;
+  P->ops_words = ops_words;
+  P->scratch_cells = scratch_cells;
+
+  // Buckets: longest work first within each, buckets in descending total work.
+  std::stable_sort(items.begin(), items.end(), [](const auto& a, const auto& b) {
+    if (!(a.first == b.first)) return a.first < b.first;
+    return a.second.work > b.second.work;
+  });
+  std::vector<uint32_t> order;
+  order.reserve(items.size());
+  P->buckets.clear();
+  std::vector<uint64_t> bwork;
+  for (size_t q = 0; q < items.size(); ++q) {
+    if (q == 0 || !(items[q].first == items[q - 1].first)) {
+      Bucket b;
+      b.kind = (PassKind)items[q].first.kind;
+      b.c = items[q].first.c;
+      b.wide = items[q].first.wide;
+      b.tb = items[q].first.tb;
+      b.lanes = items[q].first.lanes;
+      b.first = (uint32_t)order.size();
+      P->buckets.push_back(b);
+      bwork.push_back(0);
+    }
+    order.push_back(items[q].second.slot);
+    P->buckets.back().count++;
+    bwork.back() += items[q].second.work;
+  }
+  // Launch shapes: persistent grids, at most what fits the device at once.  Wide buckets
+  // may run concurrently (fan-out streams), so each gets its own scratch slice.
+  int wide_warps = 0;
+  uint64_t scratch_total = 0;
+  for (auto& b : P->buckets) {
+    if (b.kind == PK_MYERS) {
+      b.block = b.c <= 4 ? 128 : (b.c <= 8 ? 64 : 32);
+      const uint64_t per_warp = (uint64_t)(32 / b.lanes);
+      const uint64_t warps = (b.count + per_warp - 1) / per_warp;
+      const uint64_t wpb = (uint64_t)b.block / 32;
+      b.grid = (int)std::min<uint64_t>((warps + wpb - 1) / wpb, (uint64_t)ctx->sms * (2048 / b.block));
+    } else {
+      b.block = 128;
+      const uint64_t blocks = (b.count + 3) / 4;
+      const uint64_t cap = b.wide ? (uint64_t)ctx->sms * 2 : (uint64_t)ctx->sms * 16;
+      b.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, cap));
+      if (b.wide) {
+        wide_warps += b.grid * 4;
+        b.scratch_off = scratch_total;
+        scratch_total += (uint64_t)b.grid * 4 * 4 * scratch_cells;
+      }
+    }
+  }
+  P->wide_warps = wide_warps;
+  // Device buffers.
+  int rc;
+  if ((rc = P->d_bytes.ensure(std::max<uint64_t>(P->pool_bytes, 16)))) return rc;
+  if ((rc = P->d_pool.ensure(P->pool_words * 4))) return rc;
+  const size_t nseq = P->seq_boff.size();
+  if ((rc = P->d_seq.ensure(nseq * 20 + 64))) return rc;
+  if ((rc = P->d_djobs.ensure(dj.size() * sizeof(DJob) + 64))) return rc;
+  if ((rc = P->d_params.ensure(dp.size() * sizeof(DParams) + 64))) return rc;
+  if ((rc = P->d_res.ensure(dj.size() * sizeof(DRes) + 64))) return rc;
+  if ((rc = P->d_tjobs.ensure(tj.size() * sizeof(TJob) + 64))) return rc;
+  if ((rc = P->d_tres.ensure(tj.size() * sizeof(TRes) + 64))) return rc;
+  if ((rc = P->d_cls.ensure(cls.size() + 64))) return rc;
+  if ((rc = P->d_mjobs.ensure(mj.size() * sizeof(MJob) + 64))) return rc;
+  if ((rc = P->d_mout.ensure(mj.size() * 4 + 64))) return rc;
+  if ((rc = P->d_tb.ensure(tb_words * 4 + 64))) return rc;
+  if ((rc = P->d_ops.ensure(ops_words * 4 + 64))) return rc;
+  if ((rc = P->d_opsc.ensure(ops_words * 4 + 64))) return rc;
+  if ((rc = P->d_offs.ensure(wlist.size() * 8 + 64))) return rc;
+  if ((rc = P->d_total.ensure(64))) return rc;
+  if ((rc = P->d_order.ensure(order.size() * 4 + 64))) return rc;
+  if ((rc = P->d_counters.ensure(P->buckets.size() * 4 + 64))) return rc;
+  if ((rc = P->d_wlist.ensure(wlist.size() * 4 + 64))) return rc;
+  if ((rc = P->d_scratch.ensure(scratch_total * 4 + 64))) return rc;
+  // Descriptors -> device (one pinned staging area, one stream).
+  const size_t seq_bytes = nseq * 20;
+  const size_t total = seq_bytes + dj.size() * (sizeof(DJob) + sizeof(DParams) + sizeof(TJob) + 1) +
+                       mj.size() * sizeof(MJob) + order.size() * 4 + wlist.size() * 4 + 1024;
+  if ((rc = P->h_stage.ensure(total))) return rc;
+  uint8_t* h = P->h_stage.as<uint8_t>();
+  size_t at = 0;
+  auto put = [&](DevBuf& d, const void* src, size_t bytes) -> int {
+    if (!bytes) return SF_OK;
+    std::memcpy(h + at, src, bytes);
+    cudaError_t e = cudaMemcpyAsync(d.p, h + at, bytes, cudaMemcpyHostToDevice, ctx->s);
+    at += (bytes + 15) & ~size_t(15);
+    return e == cudaSuccess ? SF_OK : fail(SF_ERR_CUDA, cudaGetErrorString(e));
+  };
+  {
+    // Sequence table: byte offsets, word offsets (both 8-byte aligned), then lengths.
+    std::vector<uint8_t> st(seq_bytes);
+    std::memcpy(st.data(), P->seq_boff.data(), nseq * 8);
+    std::memcpy(st.data() + nseq * 8, P->seq_woff.data(), nseq * 8);
+    std::memcpy(st.data() + nseq * 16, P->seq_len.data(), nseq * 4);
+    if ((rc = put(P->d_seq, st.data(), seq_bytes))) return rc;
+  }
+  if ((rc = put(P->d_djobs, dj.data(), dj.size() * sizeof(DJob)))) return rc;
+  if ((rc = put(P->d_params, dp.data(), dp.size() * sizeof(DParams)))) return rc;
+  if ((rc = put(P->d_tjobs, tj.data(), tj.size() * sizeof(TJob)))) return rc;
+  if ((rc = put(P->d_cls, cls.data(), cls.size()))) return rc;
+  if ((rc = put(P->d_mjobs, mj.data(), mj.size() * sizeof(MJob)))) return rc;
+  if ((rc = put(P->d_order, order.data(), order.size() * 4))) return rc;
+  if ((rc = put(P->d_wlist, wlist.data(), wlist.size() * 4))) return rc;
+  // The pool's slack words stay zero.
+  CK(cudaMemsetAsync(P->d_pool.p, 0, P->pool_words * 4, ctx->s));
+  CK(cudaStreamSynchronize(ctx->s));  // staging is reused by the next upload
+  if (P->graph) {
+    cudaGraphExecDestroy(P->graph);
+    P->graph = nullptr;
+  }
+  P->graph_tried = false;
+  // Description.
+  std::string d = "{\"buckets\": [";
+  for (size_t q = 0; q < P->buckets.size(); ++q) {
+    const Bucket& b = P->buckets[q];
+    char buf[256];
+    std::snprintf(buf, sizeof buf,
+                  "%s{\"kind\": \"%s\", \"c\": %d, \"wide\": %s, \"traceback\": %s, \"lanes\": %d, "
+                  "\"jobs\": %u, \"grid\": %d, \"block\": %d, \"work\": %llu}",
+                  q ? ", " : "", b.kind == PK_MYERS ? "myers" : "affine", b.c,
+                  b.wide ? "true" : "false", b.tb ? "true" : "false", b.lanes, b.count, b.grid,
+                  b.block, (unsigned long long)bwork[q]);
+    d += buf;
+  }
+  d += "], \"pool_words\": " + std::to_string(P->pool_words) +
+       ", \"traceback_bytes\": " + std::to_string(tb_words * 4) + "}";
+  P->desc = d;
+  return SF_OK;
+}
+
+// Launches one execute.  With `evs`, everything runs in order on `s` with an event recorded
+// after each stage (pack, each bucket, walk + compaction) for per-stage timing.
+int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = nullptr) {
+  sf_context* ctx = P->ctx;
+  uint64_t launches = 0;
+  auto mark = [&]() -> int {
+    if (!evs) return SF_OK;
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    evs->push_back(e);
+    CK(cudaEventRecord(e, s));
+    return SF_OK;
+  };
+  int mrc;
+  if ((mrc = mark())) return mrc;
+  CK(cudaMemsetAsync(P->d_counters.p, 0, P->buckets.size() * 4 + 4, s));
+  {
+    const size_t nseq = P->seq_boff.size();
+    sfk::PackLaunch pl;
+    pl.bytes = P->d_bytes.as<uint8_t>();
+    pl.byte_off = P->d_seq.as<uint64_t>();
+    pl.word_off = reinterpret_cast<const uint64_t*>(P->d_seq.as<uint8_t>() + nseq * 8);
+    pl.len = reinterpret_cast<const uint32_t*>(P->d_seq.as<uint8_t>() + nseq * 16);
+    pl.nseq = (uint32_t)nseq;
+    pl.pool = P->d_pool.as<uint32_t>();
+    CK(sfk::launch_pack(pl, s));
+    launches += nseq ? 1 : 0;
+  }
+  if ((mrc = mark())) return mrc;
+  // Buckets fan out over the auxiliary streams so that their tails overlap.
+  const int nb = (int)P->buckets.size();
+  const int fan = evs ? 1 : std::min(nb, sf_context::kAux);
+  if (fan > 1) CK(cudaEventRecord(ctx->fork, s));
+  for (int q = 0; q < nb; ++q) {
+    const Bucket& b = P->buckets[q];
+    cudaStream_t bs = s;
+    if (fan > 1) {
+      bs = ctx->aux[q % fan];
+      if (q < fan) CK(cudaStreamWaitEvent(bs, ctx->fork, 0));
+    }
+    uint32_t* counter = P->d_counters.as<uint32_t>() + q;
+    const uint32_t* order = P->d_order.as<uint32_t>() + b.first;
+    if (b.kind == PK_MYERS) {
+      sfk::MyersLaunch ml;
+      ml.jobs = P->d_mjobs.as<MJob>();
+      ml.order = order;
+      ml.njobs = b.count;
+      ml.counter = counter;
+      ml.pool = P->d_pool.as<uint32_t>();
+      ml.out = P->d_mout.as<uint32_t>();
+      ml.lanes = b.lanes;
+      CK(sfk::launch_myers(b.c, ml, b.grid, b.block, bs));
+    } else {
+      sfk::AffLaunch al;
+      al.jobs = P->d_djobs.as<DJob>();
+      al.params = P->d_params.as<DParams>();
+      al.order = order;
+      al.njobs = b.count;
+      al.counter = counter;
+      al.pool = P->d_pool.as<uint32_t>();
+      al.bytes = P->d_bytes.as<uint8_t>();
+      al.out = P->d_res.as<DRes>();
+      al.tb = P->d_tb.as<uint32_t>();
+      al.scratch = P->d_scratch.as<int32_t>() + b.scratch_off;
+      al.scratch_cells = P->scratch_cells;
+      CK(sfk::launch_affine(b.c, b.wide, b.tb, al, b.grid, b.block, bs));
+    }
+    launches++;
+    if ((mrc = mark())) return mrc;
+  }
+  if (fan > 1) {
+    for (int i = 0; i < fan; ++i) {
+      CK(cudaEventRecord(ctx->join[i], ctx->aux[i]));
+      CK(cudaStreamWaitEvent(s, ctx->join[i], 0));
+    }
+  }
+  if (P->n_walk) {
+    sfk::WalkLaunch wl;
+    wl.jobs = P->d_djobs.as<DJob>();
+    wl.params = P->d_params.as<DParams>();
+    wl.res = P->d_res.as<DRes>();
+    wl.tjobs = P->d_tjobs.as<TJob>();
+    wl.list = P->d_wlist.as<uint32_t>();
+    wl.cls = P->d_cls.as<uint8_t>();
+    wl.nlist = P->n_walk;
+    wl.pool = P->d_pool.as<uint32_t>();
+    wl.tb = P->d_tb.as<uint32_t>();
+    wl.ops = P->d_ops.as<uint32_t>();
+    wl.tres = P->d_tres.as<TRes>();
+    CK(sfk::launch_walk(wl, s));
+    CK(sfk::launch_compact(P->d_tres.as<TRes>(), P->d_tjobs.as<TJob>(), P->d_wlist.as<uint32_t>(),
+                           P->n_walk, P->d_offs.as<uint64_t>(), P->d_ops.as<uint32_t>(),
+                           P->d_opsc.as<uint32_t>(), P->d_total.as<uint64_t>(), s));
+    launches += 3;
+  }
+  if ((mrc = mark())) return mrc;
+  P->launches = launches;
+  return SF_OK;
+}
+
+int plan_execute(sf_plan* P, bool use_graph) {
+  sf_context* ctx = P->ctx;
+  CK(cudaSetDevice(ctx->dev));
+  if (use_graph && !P->graph && !P->graph_tried) {
+    P->graph_tried = true;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal));
+    int rc = plan_launch(P, ctx->s);
+    cudaError_t e = cudaStreamEndCapture(ctx->s, &g);
+    if (rc != SF_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(SF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&P->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      P->graph = nullptr;
+      return fail(SF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+  }
+  if (use_graph && P->graph) {
+    CK(cudaGraphLaunch(P->graph, ctx->s));
+    return SF_OK;
+  }
+  return plan_launch(P, ctx->s);
+}
+
+int plan_upload_from(sf_plan* P, const uint8_t* pool) {
+  sf_context* ctx = P->ctx;
+  CK(cudaSetDevice(ctx->dev));
+  if (!P->pool_bytes) return SF_OK;
+  if (!pool) return fail(SF_ERR_INVALID, "null pool");
+  cudaPointerAttributes at{};
+  cudaError_t e = cudaPointerGetAttributes(&at, pool);
+  if (e != cudaSuccess) (void)cudaGetLastError();
+  CK(cudaMemcpyAsync(P->d_bytes.p, pool, P->pool_bytes, cudaMemcpyHostToDevice, ctx->s));
+  return SF_OK;
+}
+
+// Results -> host pinned buffers (and compacted ops), then the caller's arrays.
+int plan_fetch(sf_plan* P) {
+  sf_context* ctx = P->ctx;
+  int rc;
+  if ((rc = P->h_res.ensure(P->n_aff * sizeof(DRes) + 64))) return rc;
+  if ((rc = P->h_mout.ensure(P->n_my * 4 + 64))) return rc;
+  if ((rc = P->h_tres.ensure(P->n_aff * sizeof(TRes) + 64))) return rc;
+  if (P->n_aff) CK(cudaMemcpyAsync(P->h_res.p, P->d_res.p, P->n_aff * sizeof(DRes), cudaMemcpyDeviceToHost, ctx->s));
+  if (P->n_my) CK(cudaMemcpyAsync(P->h_mout.p, P->d_mout.p, P->n_my * 4, cudaMemcpyDeviceToHost, ctx->s));
+  if (P->n_walk) {
+    CK(cudaMemcpyAsync(P->h_tres.p, P->d_tres.p, P->n_aff * sizeof(TRes), cudaMemcpyDeviceToHost, ctx->s));
+  }
+  CK(cudaStreamSynchronize(ctx->s));
+  return SF_OK;
+}
+
+struct Fetched {
+  uint64_t ops_total = 0;
+};
+
+int plan_fetch_ops(sf_plan* P, uint64_t& total) {
+  sf_context* ctx = P->ctx;
+  total = 0;
+  if (!P->n_walk) return SF_OK;
+  CK(cudaMemcpy(&total, P->d_total.p, 8, cudaMemcpyDeviceToHost));
+  int rc;
+  if ((rc = P->h_ops.ensure(total * 4 + 64))) return rc;
+  if (total) CK(cudaMemcpyAsync(P->h_ops.p, P->d_opsc.p, total * 4, cudaMemcpyDeviceToHost, ctx->s));
+  CK(cudaStreamSynchronize(ctx->s));
+  return SF_OK;
+}
+
+// ---- one-call entry points --------------------------------------------------------------
+
+struct OneCall {
+  int device = -1;
+  sf_plan plan;
+  std::vector<uint8_t> dummy;
+  ~OneCall() { plan.ctx = nullptr; }
+};
+
+thread_local std::unique_ptr<sf_context> t_ctx;
+thread_local std::unique_ptr<OneCall> t_one;
+thread_local int t_device = -1;
+
+int one_ctx(sf_plan*& P) {
+  if (!t_ctx) {
+    int dev = t_device;
+    if (dev < 0) {
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(SF_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+      }
+    }
+    sf_context* c = nullptr;
+    int rc = make_context(dev, &c);
+    if (rc) return rc;
+    t_ctx.reset(c);
+    t_one.reset(new OneCall);
+    t_one->plan.ctx = c;
+  }
+  P = &t_one->plan;
+  return SF_OK;
+}
+
+// Sequences of one call: gathered into pinned staging as one pool.
+struct Gather {
+  std::vector<std::pair<const uint8_t*, uint64_t>> parts;
+  uint64_t bytes = 0;
+  uint64_t add(const uint8_t* p, uint64_t n) {
+    const uint64_t off = bytes;
+    parts.push_back({p, n});
+    bytes += n;
+    return off;
+  }
+};
+
+// Runs the passes of one call; res/mout/tres filled per pass (by pass index).
+int run_passes(std::vector<Pass>& passes, const Gather& g, std::vector<DRes>* res,
+               std::vector<uint32_t>* mout, std::vector<TRes>* tres, std::vector<uint32_t>* ops,
+               std::vector<uint64_t>* ops_at) {
+  sf_plan* P = nullptr;
+  int rc = one_ctx(P);
+  if (rc) return rc;
+  for (const Pass& p : passes)
+    if (p.m >= 0x7fffffffu || p.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+  P->passes = passes;
+  P->pool_bytes = g.bytes;
+  if ((rc = plan_build(P))) return rc;
+  // Pool: gather into pinned staging, then one copy.
+  if (g.bytes) {
+    if ((rc = P->h_stage.ensure(g.bytes))) return rc;
+    uint8_t* h = P->h_stage.as<uint8_t>();
+    uint64_t at = 0;
+    for (auto& pr : g.parts) {
+      if (pr.second) std::memcpy(h + at, pr.first, pr.second);
+      at += pr.second;
+    }
+    CK(cudaMemcpyAsync(P->d_bytes.p, h, g.bytes, cudaMemcpyHostToDevice, P->ctx->s));
+  }
+  if ((rc = plan_execute(P, false))) return rc;
+  if ((rc = plan_fetch(P))) return rc;
+  uint64_t total = 0;
+  if ((rc = plan_fetch_ops(P, total))) return rc;
+  const size_t np = passes.size();
+  if (res) res->assign(np, DRes{});
+  if (mout) mout->assign(np, 0);
+  if (tres) tres->assign(np, TRes{});
+  if (ops_at) ops_at->assign(np, 0);
+  std::vector<uint64_t> offs;
+  if (ops && P->n_walk) {
+    // Compacted order = walk-list order; recompute offsets on the host.
+    offs.assign(P->n_aff, 0);
+    uint64_t acc = 0;
+    const TRes* tr = P->h_tres.as<TRes>();
+    for (size_t q = 0; q < np; ++q) {
+      const Pass& p = passes[q];
+      if (p.kind == PK_MYERS || !p.want_cigar) continue;
+      const uint32_t s = P->slot[q];
+      offs[s] = acc;
+      if (tr[s].status == 0) acc += tr[s].n_ops;
+    }
+    ops->assign(P->h_ops.as<uint32_t>(), P->h_ops.as<uint32_t>() + total);
+  }
+  for (size_t q = 0; q < np; ++q) {
+    const uint32_t s = P->slot[q];
+    if (passes[q].kind == PK_MYERS) {
+      if (mout) (*mout)[q] = P->h_mout.as<uint32_t>()[s];
+    } else {
+      if (res) (*res)[q] = P->h_res.as<DRes>()[s];
+      if (tres && passes[q].want_cigar) (*tres)[q] = P->h_tres.as<TRes>()[s];
+      if (ops_at && passes[q].want_cigar && !offs.empty()) (*ops_at)[q] = offs[s];
+    }
+  }
+  return SF_OK;
+}
+
+void count_dp(const std::vector<Pass>& passes, const std::vector<DRes>& res) {
+  for (size_t q = 0; q < passes.size(); ++q)
+    if (passes[q].kind == PK_AFFINE) {
+      g_dp_cells += res[q].cells;
+      g_dp_rows += res[q].rows;
+    }
+}
+
+bool ok_mode(int mode) { return mode == SF_INFIX || mode == SF_PREFIX || mode == SF_GLOBAL; }
+bool ok_sc(const sf_affine_t* sc) {
+  // align.rs:2504 debug_assert!(open >= 0 && ext >= 0).
+  return sc && sc->open >= 0 && sc->ext >= 0;
+}
+
+Pass affine_pass(uint64_t p_off, uint64_t m, uint64_t t_off, uint64_t n, int mode,
+                 const sf_affine_t* sc, uint64_t band) {
+  Pass p;
+  p.kind = PK_AFFINE;
+  p.mode = (uint8_t)mode;
+  p.p_off = p_off;
+  p.t_off = t_off;
+  p.m = (uint32_t)m;
+  p.n = (uint32_t)n;
+  p.band = band;
+  p.geom = n;
+  p.sc = *sc;
+  return p;
+}
+
+}  // namespace
+
+// ---- C ABI ------------------------------------------------------------------------------
+
+extern "C" {
+
+const char* sf_last_error(void) { return g_err.c_str(); }
+
+const char* sf_version(void) {
+  return "spearfish_gb300 sf_align 0.1 (sm_103a; affine C={4,8,12,16,24,32,48}+wide; "
+         "myers B={1,2,3,4,6,8,12,16})";
+}
+
+int sf_set_device(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    (void)cudaGetLastError();
+    return fail(SF_ERR_INVALID, "no such device");
+  }
+  if (t_device != device) {
+    t_one.reset();
+    t_ctx.reset();
+    t_device = device;
+  }
+  return SF_OK;
+}
+
+int sf_context_create(int device, sf_context** out) {
+  if (!out) return fail(SF_ERR_INVALID, "null out");
+  return make_context(device, out);
+}
+
+void sf_context_destroy(sf_context* ctx) { delete ctx; }
+
+int sf_distance(const uint8_t* pattern, uint64_t m, const uint8_t* text, uint64_t n, int mode,
+                uint32_t k, uint32_t* out) {
+  if (!out || !ok_mode(mode) || (m && !pattern) || (n && !text)) return fail(SF_ERR_INVALID, "bad argument");
+  Gather g;
+  Pass p;
+  p.kind = PK_MYERS;
+  p.mode = (uint8_t)mode;
+  p.k = k;
+  p.p_off = g.add(pattern, m);
+  p.t_off = g.add(text, n);
+  p.m = (uint32_t)m;
+  p.n = (uint32_t)n;
+  std::vector<Pass> ps{p};
+  std::vector<uint32_t> mo;
+  int rc = run_passes(ps, g, nullptr, &mo, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  *out = mo[0];
+  return SF_OK;
+}
+
+int sf_infix_distance(const uint8_t* pattern, uint64_t m, const uint8_t* text, uint64_t n,
+                      uint32_t* out) {
+  return sf_distance(pattern, m, text, n, SF_INFIX, SF_NONE, out);
+}
+
+int sf_batch_distances(const uint8_t* pattern, uint64_t m, const uint8_t* const* texts,
+                       const uint64_t* lens, uint64_t count, int mode, uint32_t k,
+                       uint32_t* out) {
+  if (!ok_mode(mode) || (count && (!texts || !lens || !out)) || (m && !pattern))
+    return fail(SF_ERR_INVALID, "bad argument");
+  if (!count) return SF_OK;
+  Gather g;
+  const uint64_t po = g.add(pattern, m);
+  std::vector<Pass> ps;
+  ps.reserve(count);
+  for (uint64_t q = 0; q < count; ++q) {
+    if (lens[q] && !texts[q]) return fail(SF_ERR_INVALID, "null text");
+    Pass p;
+    p.kind = PK_MYERS;
+    p.mode = (uint8_t)mode;
+    p.k = k;
+    p.p_off = po;
+    p.m = (uint32_t)m;
+    p.t_off = g.add(texts[q], lens[q]);
+    p.n = (uint32_t)lens[q];
+    ps.push_back(p);
+  }
+  std::vector<uint32_t> mo;
+  int rc = run_passes(ps, g, nullptr, &mo, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  std::memcpy(out, mo.data(), count * 4);
+  return SF_OK;
+}
+
+int sf_affine(const uint8_t* pattern, uint64_t m, const uint8_t* text, uint64_t n, int mode,
+              const sf_affine_t* sc, uint64_t band, int32_t* out) {
+  if (!out || !ok_mode(mode) || !ok_sc(sc) || (m && !pattern) || (n && !text))
+    return fail(SF_ERR_INVALID, "bad argument");
+  Gather g;
+  const uint64_t po = g.add(pattern, m), to = g.add(text, n);
+  std::vector<Pass> ps{affine_pass(po, m, to, n, mode, sc, band)};
+  std::vector<DRes> r;
+  int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  count_dp(ps, r);
+  *out = r[0].score;
+  return SF_OK;
+}
+
+int sf_affine_extend(const uint8_t* pattern, uint64_t m, const uint8_t* text, uint64_t n,
+                     const sf_affine_t* sc, uint64_t band, int32_t end_bonus, int32_t xdrop,
+                     int32_t* out) {
+  if (!out || !ok_sc(sc) || (m && !pattern) || (n && !text)) return fail(SF_ERR_INVALID, "bad argument");
+  Gather g;
+  const uint64_t po = g.add(pattern, m), to = g.add(text, n);
+  Pass p = affine_pass(po, m, to, n, SF_PREFIX, sc, band);
+  p.clip = true;
+  p.xdrop = xdrop;
+  p.cell = false;
+  std::vector<Pass> ps{p};
+  std::vector<DRes> r;
+  int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  count_dp(ps, r);
+  // align.rs:728
+  *out = std::max(r[0].clip_best, sat_add32(r[0].score, end_bonus));
+  return SF_OK;
+}
+
+int sf_affine_extend_window(const uint8_t* pattern, uint64_t m, const uint8_t* text, uint64_t n,
+                            uint64_t window, const sf_affine_t* sc, uint64_t band,
+                            int32_t end_bonus, int32_t xdrop, sf_extend_t* out) {
+  if (!out || !ok_sc(sc) || (m && !pattern) || (n && !text)) return fail(SF_ERR_INVALID, "bad argument");
+  Gather g;
+  const uint64_t po = g.add(pattern, m), to = g.add(text, n);
+  Pass p = affine_pass(po, m, to, n, SF_PREFIX, sc, band);
+  p.clip = true;
+  p.cell = true;
+  p.xdrop = xdrop;
+  p.geom = std::max<uint64_t>(window, n);
+  std::vector<Pass> ps{p};
+  std::vector<DRes> r;
+  int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  count_dp(ps, r);
+  // align.rs:975-981
+  const DRes& d = r[0];
+  const int32_t whole = sat_add32(d.score, end_bonus);
+  std::memset(out, 0, sizeof *out);
+  if (d.clip_best >= whole) {
+    out->score = d.clip_best;
+    out->pattern_bases = d.clip_i;
+    out->text_bases = d.clip_j;
+  } else {
+    out->score = whole;
+    out->pattern_bases = m;
+    out->text_bases = d.score_col;
+  }
+  out->text_read = d.text_read;
+  return SF_OK;
+}
+
+int sf_affine_sorted(const uint8_t* pattern, uint64_t m, const uint8_t* const* texts,
+                     const uint64_t* lens, uint64_t count, int mode, const sf_affine_t* sc,
+                     uint64_t band, int32_t* out) {
+  if (!ok_mode(mode) || !ok_sc(sc) || (count && (!texts || !lens || !out)) || (m && !pattern))
+    return fail(SF_ERR_INVALID, "bad argument");
+  if (!count) return SF_OK;
+  Gather g;
+  const uint64_t po = g.add(pattern, m);
+  std::vector<Pass> ps;
+  for (uint64_t q = 0; q < count; ++q) {
+    const uint64_t to = g.add(texts[q], lens[q]);
+    ps.push_back(affine_pass(po, m, to, lens[q], mode, sc, band));
+  }
+  std::vector<DRes> r;
+  int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  count_dp(ps, r);
+  for (uint64_t q = 0; q < count; ++q) out[q] = r[q].score;
+  return SF_OK;
+}
+
+int sf_affine_extend_sorted_cut_bonus(const uint8_t* pattern, uint64_t m,
+                                      const uint8_t* const* texts, const uint64_t* lens,
+                                      uint64_t count, const sf_affine_t* sc, uint64_t band,
+                                      int32_t end_bonus, int32_t xdrop, int diagonal,
+                                      uint64_t window, uint64_t cut, int track_cut,
+                                      int bonus_within_cut, sf_cut_t* out) {
+  if (!ok_sc(sc) || (count && (!texts || !lens || !out)) || (m && !pattern))
+    return fail(SF_ERR_INVALID, "bad argument");
+  if (!count) return SF_OK;
+  Gather g;
+  const uint64_t po = g.add(pattern, m);
+  std::vector<Pass> ps;
+  for (uint64_t q = 0; q < count; ++q) {
+    const uint64_t n = lens[q];
+    const uint64_t to = g.add(texts[q], n);
+    Pass p = affine_pass(po, m, to, n, SF_PREFIX, sc, band);
+    // align.rs:917-928
+    p.geom = diagonal ? std::min<uint64_t>(m, n) : std::max<uint64_t>(n, window);
+    p.clip = true;
+    p.xdrop = xdrop;
+    p.cell = track_cut && cut != SF_NOLIMIT;
+    p.cut = cut;
+    ps.push_back(p);
+  }
+  std::vector<DRes> r;
+  int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  count_dp(ps, r);
+  for (uint64_t q = 0; q < count; ++q) {
+    // align.rs:929-948
+    const DRes& d = r[q];
+    const int32_t end = (bonus_within_cut && cut != SF_NOLIMIT)
+                            ? std::max(d.score, sat_add32(d.cut_score, end_bonus))
+                            : sat_add32(d.score, end_bonus);
+    const int32_t whole = std::max(d.clip_best, end);
+    out[q].whole = whole;
+    out[q].cols = d.clip_best >= end ? d.clip_j : d.score_col;
+    out[q].cut = cut == SF_NOLIMIT ? whole : std::max(d.cut_best, sat_add32(d.cut_score, end_bonus));
+  }
+  return SF_OK;
+}
+
+int sf_affine_extend_sorted_cut(const uint8_t* pattern, uint64_t m, const uint8_t* const* texts,
+                                const uint64_t* lens, uint64_t count, const sf_affine_t* sc,
+                                uint64_t band, int32_t end_bonus, int32_t xdrop, int diagonal,
+                                uint64_t window, uint64_t cut, sf_cut_t* out) {
+  // align.rs:891-900
+  return sf_affine_extend_sorted_cut_bonus(pattern, m, texts, lens, count, sc, band, end_bonus,
+                                           xdrop, diagonal, window, cut, 1, 0, out);
+}
+
+int sf_local_band_ends(const uint8_t* read, uint64_t m, const uint8_t* text, uint64_t n,
+                       const sf_affine_t* sc, int64_t dlo, int64_t dhi, int32_t bonus_start,
+                       int32_t bonus_end, int32_t* out) {
+  if (!out || !ok_sc(sc) || (m && !read) || (n && !text)) return fail(SF_ERR_INVALID, "bad argument");
+  if (m == 0 || dlo > dhi) {  // align.rs:791-793
+    *out = 0;
+    return SF_OK;
+  }
+  Gather g;
+  Pass p;
+  p.kind = PK_LOCAL;
+  p.p_off = g.add(read, m);
+  p.t_off = g.add(text, n);
+  p.m = (uint32_t)m;
+  p.n = (uint32_t)n;
+  p.dlo = dlo;
+  p.dhi = dhi;
+  p.bonus0 = bonus_start;
+  p.bonus1 = bonus_end;
+  p.sc = *sc;
+  std::vector<Pass> ps{p};
+  std::vector<DRes> r;
+  int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  *out = r[0].score;
+  return SF_OK;
+}
+
+int sf_local_band(const uint8_t* read, uint64_t m, const uint8_t* text, uint64_t n,
+                  const sf_affine_t* sc, int64_t dlo, int64_t dhi, int32_t end_bonus,
+                  int32_t* out) {
+  return sf_local_band_ends(read, m, text, n, sc, dlo, dhi, end_bonus, end_bonus, out);
+}
+
+void sf_dp_work(uint64_t* cells, uint64_t* rows) {
+  if (cells) *cells = g_dp_cells;
+  if (rows) *rows = g_dp_rows;
+}
+
+static int cigar_call(Pass p, const Gather& g, uint32_t* ops, uint64_t cap, sf_cigar_t* out,
+                      int32_t score_adjust_bonus) {
+  (void)score_adjust_bonus;
+  p.want_cigar = true;
+  std::vector<Pass> ps{p};
+  std::vector<DRes> r;
+  std::vector<TRes> t;
+  std::vector<uint32_t> o;
+  std::vector<uint64_t> at;
+  int rc = run_passes(ps, g, &r, nullptr, &t, &o, &at);
+  if (rc) return rc;
+  count_dp(ps, r);
+  std::memset(out, 0, sizeof *out);
+  out->score = t[0].score;
+  out->status = t[0].status;
+  out->pattern_end = t[0].end_i;
+  out->text_start = t[0].text_start;
+  out->text_end = t[0].end_j;
+  out->n_ops = t[0].n_ops;
+  if (t[0].status == 0) {
+    if (t[0].n_ops > cap) {
+      out->status = -1;
+      return fail(SF_ERR_CAPACITY, "CIGAR longer than the ops buffer");
+    }
+    if (t[0].n_ops) std::memcpy(ops, o.data() + at[0], t[0].n_ops * 4);
+  }
+  return SF_OK;
+}
+
+int sf_affine_cigar(const uint8_t* pattern, uint64_t m, const uint8_t* text, uint64_t n,
+                    int mode, const sf_affine_t* sc, uint64_t band, uint32_t* ops, uint64_t cap,
+                    sf_cigar_t* out) {
+  if (!out || !ok_mode(mode) || !ok_sc(sc) || (m && !pattern) || (n && !text) || (cap && !ops))
+    return fail(SF_ERR_INVALID, "bad argument");
+  Gather g;
+  const uint64_t po = g.add(pattern, m), to = g.add(text, n);
+  Pass p = affine_pass(po, m, to, n, mode, sc, band);
+  p.tb_kind = 0;
+  return cigar_call(p, g, ops, cap, out, 0);
+}
+
+int sf_affine_extend_window_cigar(const uint8_t* pattern, uint64_t m, const uint8_t* text,
+                                  uint64_t n, uint64_t window, const sf_affine_t* sc,
+                                  uint64_t band, int32_t end_bonus, int32_t xdrop, uint32_t* ops,
+                                  uint64_t cap, sf_cigar_t* out) {
+  if (!out || !ok_sc(sc) || (m && !pattern) || (n && !text) || (cap && !ops))
+    return fail(SF_ERR_INVALID, "bad argument");
+  Gather g;
+  const uint64_t po = g.add(pattern, m), to = g.add(text, n);
+  Pass p = affine_pass(po, m, to, n, SF_PREFIX, sc, band);
+  p.clip = true;
+  p.cell = true;
+  p.xdrop = xdrop;
+  p.geom = std::max<uint64_t>(window, n);
+  p.tb_kind = 1;
+  p.end_bonus = end_bonus;
+  return cigar_call(p, g, ops, cap, out, end_bonus);
+}
+
+// ---- plans ------------------------------------------------------------------------------
+
+static int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
+                          uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps) {
+  ps.clear();
+  ps.reserve(count);
+  for (uint64_t q = 0; q < count; ++q) {
+    const sf_job_t& j = jobs[q];
+    Pass p;
+    p.p_off = j.p_off;
+    p.t_off = j.t_off;
+    p.m = j.m;
+    p.n = j.n;
+    if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+    if (j.p_off + j.m > pool_bytes || j.t_off + j.n > pool_bytes)
+      return fail(SF_ERR_INVALID, "job sequence outside the pool");
+    if (j.kind != SF_JOB_MYERS) {
+      if (j.sc_index >= n_scores || !ok_sc(&scores[j.sc_index]))
+        return fail(SF_ERR_INVALID, "bad scoring index");
+      p.sc = scores[j.sc_index];
+    }
+    switch (j.kind) {
+      case SF_JOB_MYERS:
+        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
+        p.kind = PK_MYERS;
+        p.mode = j.mode;
+        p.k = j.k;
+        break;
+      case SF_JOB_AFFINE:
+        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
+        p.kind = PK_AFFINE;
+        p.mode = j.mode;
+        p.band = j.band;
+        p.geom = j.n;
+        p.want_cigar = j.want_cigar != 0;
+        p.tb_kind = 0;
+        break;
+      case SF_JOB_EXTEND_WINDOW:
+        p.kind = PK_AFFINE;
+        p.mode = SF_PREFIX;
+        p.band = j.band;
+        p.geom = std::max<uint64_t>(j.window, j.n);
+        p.clip = true;
+        p.cell = true;
+        p.xdrop = j.xdrop;
+        p.end_bonus = j.end_bonus;
+        p.want_cigar = j.want_cigar != 0;
+        p.tb_kind = 1;
+        break;
+      case SF_JOB_LOCAL:
+        p.kind = PK_LOCAL;
+        p.dlo = j.dlo;
+        p.dhi = j.dhi;
+        p.bonus0 = j.end_bonus;
+        p.bonus1 = j.end_bonus2;
+        break;
+      default:
+        return fail(SF_ERR_INVALID, "bad job kind");
+    }
+    ps.push_back(p);
+  }
+  return SF_OK;
+}
+
+int sf_plan_create(sf_context* ctx, const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
+                   uint32_t n_scores, uint64_t pool_bytes, sf_plan** out) {
+  if (!ctx || !out || (count && !jobs)) return fail(SF_ERR_INVALID, "bad argument");
+  std::unique_ptr<sf_plan> P(new sf_plan);
+  P->ctx = ctx;
+  P->pool_bytes = pool_bytes;
+  int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes);
+  if (rc) return rc;
+  if ((rc = plan_build(P.get()))) return rc;
+  *out = P.release();
+  return SF_OK;
+}
+
+void sf_plan_destroy(sf_plan* plan) { delete plan; }
+
+int sf_plan_upload(sf_plan* plan, const uint8_t* pool) {
+  if (!plan) return fail(SF_ERR_INVALID, "null plan");
+  return plan_upload_from(plan, pool);
+}
+
+int sf_plan_execute(sf_plan* plan) {
+  if (!plan) return fail(SF_ERR_INVALID, "null plan");
+  return plan_execute(plan, true);
+}
+
+int sf_plan_sync(sf_plan* plan) {
+  if (!plan) return fail(SF_ERR_INVALID, "null plan");
+  CK(cudaSetDevice(plan->ctx->dev));
+  CK(cudaStreamSynchronize(plan->ctx->s));
+  return SF_OK;
+}
+
+void* sf_plan_stream(sf_plan* plan) { return plan ? (void*)plan->ctx->s : nullptr; }
+
+uint64_t sf_plan_launches(const sf_plan* plan) { return plan ? plan->launches : 0; }
+
+const char* sf_plan_describe(sf_plan* plan) { return plan ? plan->desc.c_str() : ""; }
+
+int sf_plan_download(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
+                     uint64_t* ops_used) {
+  if (!P || (!results && !P->passes.empty())) return fail(SF_ERR_INVALID, "bad argument");
+  CK(cudaSetDevice(P->ctx->dev));
+  int rc = plan_fetch(P);
+  if (rc) return rc;
+  uint64_t total = 0;
+  if ((rc = plan_fetch_ops(P, total))) return rc;
+  if (ops_used) *ops_used = total;
+  if (total && (!ops || ops_cap < total)) {
+    if (ops_used) *ops_used = total;
+    return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
+  }
+  if (total) std::memcpy(ops, P->h_ops.p, total * 4);
+  const DRes* rs = P->h_res.as<DRes>();
+  const TRes* tr = P->h_tres.as<TRes>();
+  const uint32_t* mo = P->h_mout.as<uint32_t>();
+  uint64_t acc = 0;
+  // Compacted op order = walk-list order = pass order among CIGAR passes.
+  for (size_t q = 0; q < P->passes.size(); ++q) {
+    const Pass& p = P->passes[q];
+    sf_result_t& o = results[q];
+    std::memset(&o, 0, sizeof o);
+    const uint32_t s = P->slot[q];
+    if (p.kind == PK_MYERS) {
+      o.distance = mo[s];
+      o.score = 0;
+      o.cells = (uint64_t)p.m * p.n;
+      continue;
+    }
+    const DRes& d = rs[s];
+    o.distance = SF_NONE;
+    o.cells = d.cells;
+    o.text_read = d.text_read;
+    if (p.kind == PK_LOCAL) {
+      o.score = d.score;
+    } else if (p.tb_kind == 1) {
+      const int32_t whole = sat_add32(d.score, p.end_bonus);
+      if (d.clip_best >= whole) {
+        o.score = d.clip_best;
+        o.pattern_end = d.clip_i;
+        o.text_end = d.clip_j;
+      } else {
+        o.score = whole;
+        o.pattern_end = p.m;
+        o.text_end = d.score_col;
+      }
+    } else {
+      o.score = d.score;
+      o.pattern_end = p.m;
+      o.text_end = d.score_col;
+    }
+    if (p.want_cigar && p.kind != PK_LOCAL) {
+      const TRes& t = tr[s];
+      o.status = t.status;
+      o.text_start = t.text_start;
+      o.cigar_off = acc;
+      o.n_ops = t.status == 0 ? t.n_ops : 0;
+      acc += o.n_ops;
+    }
+  }
+  return SF_OK;
+}
+
+int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, const sf_job_t* jobs,
+                 uint64_t count, const sf_affine_t* scores, uint32_t n_scores,
+                 sf_result_t* results, uint32_t* ops, uint64_t ops_cap, uint64_t* ops_used) {
+  if (!ctx || (count && (!jobs || !results))) return fail(SF_ERR_INVALID, "bad argument");
+  // The context keeps one plan whose device and pinned buffers grow and are reused, so a
+  // stream of batches allocates only when a batch outgrows the last.
+  if (!ctx->cache) {
+    ctx->cache.reset(new sf_plan);
+    ctx->cache->ctx = ctx;
+  }
+  sf_plan* P = ctx->cache.get();
+  int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes);
+  if (rc) return rc;
+  P->pool_bytes = pool_bytes;
+  if ((rc = plan_build(P))) return rc;
+  if ((rc = plan_upload_from(P, pool))) return rc;
+  if ((rc = plan_execute(P, false))) return rc;
+  return sf_plan_download(P, results, ops, ops_cap, ops_used);
+}
+
+int sf_plan_profile(sf_plan* P, float* ms, uint32_t cap, uint32_t* n_stages) {
+  if (!P || !n_stages || (cap && !ms)) return fail(SF_ERR_INVALID, "bad argument");
+  CK(cudaSetDevice(P->ctx->dev));
+  std::vector<cudaEvent_t> evs;
+  int rc = plan_launch(P, P->ctx->s, &evs);
+  cudaError_t e = cudaStreamSynchronize(P->ctx->s);
+  const uint32_t n = evs.empty() ? 0 : (uint32_t)evs.size() - 1;
+  *n_stages = n;
+  for (uint32_t q = 0; q < n && q < cap && rc == SF_OK && e == cudaSuccess; ++q) {
+    float t = 0;
+    cudaEventElapsedTime(&t, evs[q], evs[q + 1]);
+    ms[q] = t;
+  }
+  for (cudaEvent_t x : evs) cudaEventDestroy(x);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(SF_ERR_CUDA, cudaGetErrorString(e));
+  return n > cap ? fail(SF_ERR_CAPACITY, "more stages than ms slots") : SF_OK;
+}
+
+int sf_int_peak(int device, double* tops, double* ms) {
+  if (!tops) return fail(SF_ERR_INVALID, "bad argument");
+  CK(cudaSetDevice(device));
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  DevBuf out;
+  int rc = out.ensure((size_t)sms * 8 * 256 * 4);
+  if (rc) return rc;
+  double best = 0, best_ms = 0;
+  for (int rep = 0; rep < 4; ++rep) {
+    float t = 0;
+    uint64_t ops = 0;
+    CK(sfk::run_int_peak(sms, out.as<int32_t>(), &t, &ops));
+    const double r = (double)ops / (t * 1e-3) / 1e12;
+    if (rep > 0 && r > best) {  // the first run warms up clocks and caches
+      best = r;
+      best_ms = t;
+    }
+  }
+  *tops = best;
+  if (ms) *ms = best_ms;
+  return SF_OK;
+}
+
+}  // extern "C"

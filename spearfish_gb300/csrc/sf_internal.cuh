@@ -1,0 +1,204 @@
+// Internal device-side definitions shared by the kernels and the host engine.
+//
+// Sequence layout in HBM: 2-bit codes, 16 bases per 32-bit word, base x at bits
+// 2*(x % 16) of word x / 16 -- the same bit order as spearfish's packed transcript store
+// (crates/index/src/lib.rs:253-280, 32 bases per u64, read as little-endian words).  Each
+// sequence starts on a word boundary and carries ONE leading pad base, so that DP row i
+// (pattern base i - 1) and DP column j (text base j - 1) read packed position i / j
+// directly, as the reference's rows and columns are numbered (align.rs:2557, 1027-1072).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sf {
+
+constexpr int32_t NEG = INT32_MIN / 4;      // align.rs:693
+constexpr int32_t NEG_INF = INT32_MIN / 2;  // "no predecessor" inside a lane's gap chain
+constexpr uint32_t FULL = 0xffffffffu;
+
+// Job flag bits (DJob::flags).
+enum : uint32_t {
+  F_MODE = 3u,        // sf_mode
+  F_CLIP = 1u << 2,   // clip = Some((xdrop, cell))
+  F_CELL = 1u << 3,   //   ... with the best cell tracked
+  F_FULL = 1u << 4,   // unbanded rows (Infix or band = usize::MAX)
+  F_TB = 1u << 5,     // write traceback nibbles
+  F_CUT = 1u << 6,    // track the cut column
+  F_LOCAL = 1u << 7,  // local band (floor 0, diagonal range, end bonuses)
+  F_ROWMAX = 1u << 8  // per-row maximum needed (clip, cut or local)
+};
+
+// One affine / local pass.  64 bytes.
+struct DJob {
+  uint64_t p_word;   // packed pattern (word offset in the pool)
+  uint64_t t_word;   // packed text
+  uint64_t p_byte;   // local band: the read's byte codes (unmasked) in the byte pool
+  int64_t below;     // banded rows: below / above (align.rs:2458-2461); local: dlo / dhi
+  int64_t above;
+  uint64_t cut;      // cut column (UINT64_MAX: none)
+  uint64_t tb_word;  // traceback nibbles: word offset in the traceback arena
+  uint32_t m, n;
+};
+
+struct DParams {
+  uint32_t flags;
+  int32_t xdrop;
+  int32_t bonus0, bonus1;  // local: start / end bonus
+  int32_t mat, mis, open, ext;
+};
+
+// What one pass found: align.rs:2111-2129 `Dp`, plus its DP_WORK cells.  48 bytes.
+struct DRes {
+  int32_t score, clip_best, cut_best, cut_score;
+  uint32_t score_col, clip_i, clip_j, text_read, last_row, rows;
+  uint64_t cells;
+};
+
+// One Myers job: align.rs:88-168 `distance`.
+struct MJob {
+  uint64_t p_word, t_word;
+  uint32_t m, n;
+  uint32_t mode, k;
+};
+
+// Traceback walk: which end cell, and where the CIGAR goes.
+struct TJob {
+  uint64_t ops_off;   // first op slot
+  uint32_t ops_cap;
+  uint32_t kind;      // 0: affine end (m, score_col); 1: extend window end
+  int32_t end_bonus;
+  uint32_t pad;
+};
+
+struct TRes {
+  int32_t score, status;
+  uint32_t end_i, end_j, text_start, n_ops;
+};
+
+__host__ __device__ inline uint32_t tb_words_per_lane(int c) { return (uint32_t)((c + 7) / 8); }
+
+// The widest row of a pass: banded rows are at most below + above + 1 cells
+// (align.rs:2458-2468), local rows at most dhi - dlo + 1 (align.rs:800-805), and no row has
+// more than the n + 1 columns of the text.
+__host__ __device__ inline int64_t band_wmax(const DJob& J, uint32_t flags) {
+  const int64_t n = J.n;
+  int64_t w;
+  if (flags & F_LOCAL)
+    w = J.above - J.below + 1;
+  else if (flags & F_FULL)
+    w = n + 1;
+  else
+    w = J.below + J.above + 1;
+  return w < 0 ? 0 : (w > n + 1 ? n + 1 : w);
+}
+
+// Traceback words of one row: `chunks` chunks of 32 lanes x ceil(C/8) words.
+__host__ __device__ inline uint64_t tb_row_words(int c, int64_t chunks) {
+  return (uint64_t)chunks * 32u * tb_words_per_lane(c);
+}
+
+// Chunks of 32*C offsets a wide row needs: its cells plus the NEG sentinel after them.
+__host__ __device__ inline int64_t wide_chunks(int c, int64_t w) {
+  return (w + 1 + 32 * c - 1) / (32 * c);
+}
+
+__device__ __forceinline__ uint32_t base_at(const uint32_t* __restrict__ pool, uint64_t word,
+                                            uint64_t pos) {
+  return (__ldg(pool + word + (pos >> 4)) >> (2 * (pos & 15))) & 3u;
+}
+
+// max(a + b, c) and 3-way max via the sm_90+ DPX integer instructions.
+__device__ __forceinline__ int32_t addmax(int32_t a, int32_t b, int32_t c) {
+  return __viaddmax_s32(a, b, c);
+}
+__device__ __forceinline__ int32_t max3(int32_t a, int32_t b, int32_t c) {
+  return __vimax3_s32(a, b, c);
+}
+__device__ __forceinline__ int32_t sat_add(int32_t a, int32_t b) {
+  long long s = (long long)a + b;
+  return s > INT32_MAX ? INT32_MAX : s < INT32_MIN ? INT32_MIN : (int32_t)s;
+}
+__device__ __forceinline__ int32_t sat_sub(int32_t a, int32_t b) {
+  long long s = (long long)a - b;
+  return s > INT32_MAX ? INT32_MAX : s < INT32_MIN ? INT32_MIN : (int32_t)s;
+}
+
+}  // namespace sf
+
+// Launch entry points implemented by the kernel translation units.
+namespace sfk {
+
+struct AffLaunch {
+  const sf::DJob* jobs;
+  const sf::DParams* params;  // per job
+  const uint32_t* order;      // job indices of this bucket, longest first
+  uint32_t njobs;
+  uint32_t* counter;          // work-queue head
+  const uint32_t* pool;
+  const uint8_t* bytes;       // byte pool (local band reads)
+  sf::DRes* out;
+  uint32_t* tb;               // traceback arena
+  int32_t* scratch;           // WIDE rows: per warp 4 * scratch_cells int32
+  uint64_t scratch_cells;
+};
+
+// C: cells per lane (register rows); wide: rows in global scratch, chunked.
+cudaError_t launch_affine(int c, bool wide, bool tb, const AffLaunch& a, int grid, int block,
+                          cudaStream_t s);
+// The C values the register kernel is built for (ascending), and the wide chunk C.
+extern const int kAffineC[];
+extern const int kAffineNC;
+constexpr int kWideC = 16;
+
+struct WalkLaunch {
+  const sf::DJob* jobs;
+  const sf::DParams* params;
+  const sf::DRes* res;
+  const sf::TJob* tjobs;
+  const uint32_t* list;   // jobs that want a CIGAR
+  const uint8_t* cls;     // per job: C value of the kernel that ran it, 0xff for wide
+  uint32_t nlist;
+  const uint32_t* pool;
+  const uint32_t* tb;
+  uint32_t* ops;
+  sf::TRes* tres;
+};
+cudaError_t launch_walk(const WalkLaunch& a, cudaStream_t s);
+
+struct MyersLaunch {
+  const sf::MJob* jobs;
+  const uint32_t* order;
+  uint32_t njobs;
+  uint32_t* counter;
+  const uint32_t* pool;
+  uint32_t* out;
+  int lanes;  // lanes per pair (power of two <= 32)
+};
+cudaError_t launch_myers(int blocks_per_lane, const MyersLaunch& a, int grid, int block,
+                         cudaStream_t s);
+extern const int kMyersB[];
+extern const int kMyersNB;
+
+struct PackLaunch {
+  const uint8_t* bytes;
+  const uint64_t* byte_off;  // per sequence
+  const uint32_t* len;
+  const uint64_t* word_off;
+  uint32_t nseq;
+  uint32_t* pool;
+};
+cudaError_t launch_pack(const PackLaunch& a, cudaStream_t s);
+
+// Exclusive scan of per-job op counts (single block) and the gather that compacts ops.
+cudaError_t launch_compact(const sf::TRes* tres, const sf::TJob* tjobs, const uint32_t* list,
+                           uint32_t nlist, uint64_t* offs, const uint32_t* ops_in,
+                           uint32_t* ops_out, uint64_t* total, cudaStream_t s);
+
+}  // namespace sfk
+
+namespace sfk {
+// INT32 throughput probe: the DP's instruction mix (add-then-max on independent chains).
+// Runs grid = sms * 8 blocks of 256 threads; returns the elapsed ms and the ops counted.
+cudaError_t run_int_peak(int sms, int32_t* out, float* ms, uint64_t* ops);
+}  // namespace sfk

@@ -1,0 +1,112 @@
+// Byte codes -> 2-bit packed sequences in HBM, and the compaction of CIGAR ops.
+//
+// Packing is HBM-bound byte work: one warp per sequence, each lane building whole 16-base
+// words from 16 consecutive bytes (coalesced 512-byte spans per warp), written once.
+#include "sf_internal.cuh"
+
+namespace {
+
+__global__ void __launch_bounds__(256) pack_kernel(sfk::PackLaunch a) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t s = warp; s < a.nseq; s += nwarps) {
+    const uint8_t* src = a.bytes + a.byte_off[s];
+    const uint64_t len = a.len[s];
+    const uint64_t words = (len + 1 + 15) / 16;  // one leading pad base
+    uint32_t* dst = a.pool + a.word_off[s];
+    for (uint64_t w = lane; w < words; w += 32) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int b = 0; b < 16; ++b) {
+        const uint64_t pos = 16 * w + b;
+        if (pos >= 1 && pos - 1 < len) v |= (uint32_t)(src[pos - 1] & 3) << (2 * b);
+      }
+      dst[w] = v;
+    }
+  }
+}
+
+// Exclusive scan of the walk's op counts over `nlist` jobs, in one block.
+__global__ void __launch_bounds__(1024) scan_kernel(const sf::TRes* tres, const uint32_t* list,
+                                                    uint32_t nlist, uint64_t* offs,
+                                                    uint64_t* total) {
+  __shared__ uint64_t warp_sums[32];
+  __shared__ uint64_t carry;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < nlist; base += 1024) {
+    const uint32_t q = base + tid;
+    uint64_t v = 0;
+    if (q < nlist) {
+      const sf::TRes r = tres[list[q]];
+      v = r.status == 0 ? r.n_ops : 0;
+    }
+    uint64_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      uint64_t y = __shfl_up_sync(sf::FULL, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      uint64_t s = warp_sums[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint64_t y = __shfl_up_sync(sf::FULL, s, d);
+        if (lane >= d) s += y;
+      }
+      warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const uint64_t before = carry + (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+    if (q < nlist) offs[q] = before;
+    __syncthreads();
+    if (tid == 1023) carry = before + v;
+    __syncthreads();
+  }
+  if (tid == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(256) gather_kernel(const sf::TRes* tres, const sf::TJob* tjobs,
+                                                     const uint32_t* list, uint32_t nlist,
+                                                     const uint64_t* offs, const uint32_t* in,
+                                                     uint32_t* out) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t q = warp; q < nlist; q += nwarps) {
+    const uint32_t j = list[q];
+    const sf::TRes r = tres[j];
+    if (r.status != 0) continue;
+    const uint32_t* src = in + tjobs[j].ops_off;
+    uint32_t* dst = out + offs[q];
+    for (uint32_t x = lane; x < r.n_ops; x += 32) dst[x] = src[x];
+  }
+}
+
+}  // namespace
+
+namespace sfk {
+
+cudaError_t launch_pack(const PackLaunch& a, cudaStream_t s) {
+  if (a.nseq == 0) return cudaSuccess;
+  const uint32_t warps = a.nseq < 152u * 64u ? a.nseq : 152u * 64u;
+  pack_kernel<<<(warps + 7) / 8, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const sf::TRes* tres, const sf::TJob* tjobs, const uint32_t* list,
+                           uint32_t nlist, uint64_t* offs, const uint32_t* ops_in,
+                           uint32_t* ops_out, uint64_t* total, cudaStream_t s) {
+  scan_kernel<<<1, 1024, 0, s>>>(tres, list, nlist, offs, total);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || nlist == 0) return e;
+  const uint32_t warps = nlist < 152u * 64u ? nlist : 152u * 64u;
+  gather_kernel<<<(warps + 7) / 8, 256, 0, s>>>(tres, tjobs, list, nlist, offs, ops_in, ops_out);
+  return cudaGetLastError();
+}
+
+}  // namespace sfk

@@ -1,0 +1,166 @@
+"""Seeded synthetic workloads in the shapes the alignment stage is benchmarked on.
+
+The error model restates spearfish's read simulator (crates/spearfish-cli/src/sim.rs:59-99):
+each base is deleted, substituted or kept, then an insertion may follow it; indel
+probabilities are raised inside homopolymer runs (length >= 3) by `hp_bias` and scaled down
+elsewhere so the mean rate stays as requested; insertions inside runs extend the run.  Random
+draws come from numpy's PCG64 seeded per workload (the reference's SplitMix64 streams are
+not reproduced: no output depends on them).
+
+Workloads (sizes as the benchmark configurations state them):
+  c1  Myers: 10,000 pairs, query uniform ACGT of 1,000 bases; target = query with 8%
+      errors (sub:ins:del = 2:1:1), plus 50 random bases on each side; Infix.
+  c2  banded affine with traceback: 20,000 pairs, query 2,000 bases; target = query with
+      10% ONT-like errors -- indel-heavy (30% substitutions, 70% indels), deletions 40% of
+      indel sites, indels raised 4x inside homopolymers; band 128, Affine{2,4,4,2}, Global.
+  c3  uneven batch: 100,000 pairs, query length log-normal (median 1,200, sigma 0.8)
+      clipped to 200..20,000; error rate uniform 5-12% with c2's profile; per pair a Myers
+      Infix job (target + 50-base flanks) and a banded affine Global job with band
+      clamp(32 * ceil(0.1 * L / 32), 64, 512).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+@dataclass(frozen=True)
+class Profile:
+    sub: float
+    ins: float
+    dele: float
+    hp_bias: float
+
+
+UNIFORM_211 = Profile(0.50, 0.25, 0.25, 1.0)  # c1: sub:ins:del = 2:1:1
+ONT_INDEL = Profile(0.30, 0.42, 0.28, 4.0)    # c2/c3: indel-heavy, del 40% of indels
+HIFI = Profile(0.20, 0.40, 0.40, 10.0)        # sim.rs:38-45 `hifi`
+
+
+def homopolymer_mask(seq: np.ndarray) -> np.ndarray:
+    """sim.rs:60-72: base i lies in a run of >= 3 equal bases."""
+    n = seq.size
+    if n == 0:
+        return np.zeros(0, dtype=bool)
+    starts = np.concatenate([[0], np.flatnonzero(np.diff(seq) != 0) + 1])
+    lens = np.diff(np.concatenate([starts, [n]]))
+    return np.repeat(lens >= 3, lens)
+
+
+def simulate(orig: np.ndarray, rate: float, p: Profile, rng: np.random.Generator) -> np.ndarray:
+    """sim.rs:59-99 `simulate`, one pass of numpy draws per base."""
+    n = orig.size
+    hp = homopolymer_mask(orig)
+    f_hp = float(hp.mean()) if n else 0.0
+    scale = 1.0 / (1.0 - f_hp + p.hp_bias * f_hp)
+    p_sub, p_ins, p_del = rate * p.sub, rate * p.ins, rate * p.dele
+    bias = scale * np.where(hp, p.hp_bias, 1.0)
+    r = rng.random(n)
+    dele = r < p_del * bias
+    subs = ~dele & (r < p_del * bias + p_sub)
+    base = orig.copy()
+    base[subs] = (orig[subs] + rng.integers(1, 4, int(subs.sum()), dtype=np.uint8)) & 3
+    keep = ~dele
+    ins = rng.random(n) < p_ins * bias
+    ins_base = np.where(hp, orig, rng.integers(0, 4, n, dtype=np.uint8)).astype(np.uint8)
+    counts = keep.astype(np.int64) + ins
+    out = np.empty(int(counts.sum()), dtype=np.uint8)
+    at = np.cumsum(counts) - counts
+    out[at[keep]] = base[keep]
+    out[(at + keep)[ins]] = ins_base[ins]
+    return out
+
+
+@dataclass
+class Pairs:
+    """Pairs as one pool of byte codes: pattern q at pool[p_off[q]:+m[q]], text likewise."""
+    pool: np.ndarray
+    p_off: np.ndarray
+    m: np.ndarray
+    t_off: np.ndarray
+    n: np.ndarray
+    band: np.ndarray      # per pair (affine)
+    name: str
+
+    def __len__(self):
+        return int(self.m.size)
+
+    def pattern(self, q: int) -> np.ndarray:
+        return self.pool[self.p_off[q]:self.p_off[q] + self.m[q]]
+
+    def text(self, q: int) -> np.ndarray:
+        return self.pool[self.t_off[q]:self.t_off[q] + self.n[q]]
+
+    def subset(self, idx) -> "Pairs":
+        idx = np.asarray(idx)
+        parts, p_off, t_off = [], [], []
+        at = 0
+        for q in idx:
+            p, t = self.pattern(int(q)), self.text(int(q))
+            p_off.append(at)
+            parts.append(p)
+            at += p.size
+            t_off.append(at)
+            parts.append(t)
+            at += t.size
+        pool = np.concatenate(parts) if parts else np.zeros(1, np.uint8)
+        return Pairs(pool, np.array(p_off, np.uint64), self.m[idx].copy(),
+                     np.array(t_off, np.uint64), self.n[idx].copy(), self.band[idx].copy(),
+                     self.name)
+
+
+def _assemble(ps, ts, bands, name) -> Pairs:
+    m = np.array([p.size for p in ps], dtype=np.uint32)
+    n = np.array([t.size for t in ts], dtype=np.uint32)
+    inter = [x for pair in zip(ps, ts) for x in pair]
+    sizes = np.array([x.size for x in inter], dtype=np.uint64)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+    pool = np.concatenate(inter) if inter else np.zeros(1, np.uint8)
+    return Pairs(pool, offs[0::2].copy(), m, offs[1::2].copy(), n,
+                 np.asarray(bands, dtype=np.uint64), name)
+
+
+def config1(pairs: int = 10_000, seed: int = 1) -> Pairs:
+    rng = np.random.default_rng(seed)
+    ps, ts = [], []
+    for _ in range(pairs):
+        q = rng.integers(0, 4, 1000, dtype=np.uint8)
+        t = simulate(q, 0.08, UNIFORM_211, rng)
+        fl = rng.integers(0, 4, 100, dtype=np.uint8)
+        ps.append(q)
+        ts.append(np.concatenate([fl[:50], t, fl[50:]]))
+    return _assemble(ps, ts, np.zeros(pairs), "c1")
+
+
+def config2(pairs: int = 20_000, seed: int = 2, m: int = 2000, band: int = 128) -> Pairs:
+    rng = np.random.default_rng(seed)
+    ps, ts = [], []
+    for _ in range(pairs):
+        q = rng.integers(0, 4, m, dtype=np.uint8)
+        ps.append(q)
+        ts.append(simulate(q, 0.10, ONT_INDEL, rng))
+    return _assemble(ps, ts, np.full(pairs, band), "c2")
+
+
+def c3_band(L: np.ndarray) -> np.ndarray:
+    """Band for a query of L bases: clamp(32 * ceil(0.1 * L / 32), 64, 512)."""
+    return np.clip(32 * np.ceil(0.1 * L / 32.0), 64, 512).astype(np.uint64)
+
+
+def config3(pairs: int = 100_000, seed: int = 3) -> tuple[Pairs, Pairs]:
+    """(Myers pairs with flanked targets, affine pairs) for the same queries."""
+    rng = np.random.default_rng(seed)
+    L = np.clip(np.round(np.exp(np.log(1200.0) + 0.8 * rng.standard_normal(pairs))), 200,
+                20000).astype(np.int64)
+    rates = rng.uniform(0.05, 0.12, pairs)
+    qs, ts, fts = [], [], []
+    for i in range(pairs):
+        q = rng.integers(0, 4, int(L[i]), dtype=np.uint8)
+        t = simulate(q, float(rates[i]), ONT_INDEL, rng)
+        fl = rng.integers(0, 4, 100, dtype=np.uint8)
+        qs.append(q)
+        ts.append(t)
+        fts.append(np.concatenate([fl[:50], t, fl[50:]]))
+    return (_assemble(qs, fts, np.zeros(pairs), "c3-myers"),
+            _assemble(qs, ts, c3_band(L.astype(np.float64)), "c3-affine"))

@@ -217,3 +217,38 @@ def check_window_relations(impl):
         u[i] = 3 - u[i]
     assert impl.affine_extend_window(p, u, len(u), a["sc"], a["band"], a["end_bonus"],
                                      a["xdrop"]) == r
+
+
+class GpuImpl:
+    """The CUDA library's one-call entry points (spearfish_gb300.align)."""
+
+    def __init__(self):
+        from spearfish_gb300 import align as A
+        self.A = A
+
+    def distance(self, p, t, mode, k=U32_MAX):
+        return self.A.distance(p, t, mode, k)
+
+    def batch_distances(self, p, texts, mode, k=U32_MAX):
+        return self.A.batch_distances(self.A.Pattern(p), texts, mode, k)
+
+    def affine(self, p, t, mode, sc, band):
+        return self.A.affine(p, t, mode, sc, band)
+
+    def affine_extend(self, p, t, sc, band, end_bonus, xdrop):
+        return self.A.affine_extend(p, t, sc, band, end_bonus, xdrop)
+
+    def affine_extend_window(self, p, t, window, sc, band, end_bonus, xdrop):
+        return self.A.affine_extend_window(p, t, window, sc, band, end_bonus, xdrop)
+
+    def affine_sorted(self, p, texts, mode, sc, band):
+        return self.A.affine_sorted(p, texts, mode, sc, band)
+
+    def affine_extend_sorted_cut_bonus(self, p, texts, sc, band, end_bonus, xdrop, diagonal,
+                                       window, cut, track_cut, bonus_within_cut):
+        return self.A.affine_extend_sorted_cut_bonus(p, texts, sc, band, end_bonus, xdrop,
+                                                     diagonal, window, cut, track_cut,
+                                                     bonus_within_cut)
+
+    def local_band_ends(self, read, t, sc, dlo, dhi, bonus):
+        return self.A.local_band_ends(read, t, sc, dlo, dhi, tuple(bonus))
