@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 GOLD = {"c1": "myers-infix-10k", "c2": "affine-global-band128-cigar-20k",
+        "c2-score": "affine-global-band128-score-20k",
         "c3": "uneven-myers+affine-100k"}
 OPS_PER_CELL = {"affine_tb": 12, "affine": 10, "myers": 0.625}
 
@@ -129,7 +130,7 @@ def make_jobs(B, pairs, kind, mode, want_cigar, band=None):
     return jobs
 
 
-def workload(cfg: str, scale: float):
+def workload(cfg: str, scale: float, cigar: bool = True):
     from spearfish_gb300 import batch as B
     from spearfish_gb300 import workloads as W
     if cfg == "c1":
@@ -137,19 +138,19 @@ def workload(cfg: str, scale: float):
         return w.pool, make_jobs(B, w, B.JOB_MYERS, 0, False), [w], "myers"
     if cfg == "c2":
         w = W.config2(int(20_000 * scale))
-        return w.pool, make_jobs(B, w, B.JOB_AFFINE, 2, True), [w], "affine_tb"
+        return w.pool, make_jobs(B, w, B.JOB_AFFINE, 2, cigar), [w], "affine_tb" if cigar else "affine"
     my, af = W.config3(int(100_000 * scale))
     # One pool: the affine pairs' offsets shift past the Myers pool.
     shift = np.uint64(my.pool.size)
     pool = np.concatenate([my.pool, af.pool])
     jm = make_jobs(B, my, B.JOB_MYERS, 0, False)
-    ja = make_jobs(B, af, B.JOB_AFFINE, 2, True)
+    ja = make_jobs(B, af, B.JOB_AFFINE, 2, cigar)
     ja["p_off"] += shift
     ja["t_off"] += shift
     return pool, np.concatenate([jm, ja]), [my, af], "mixed"
 
 
-AFFINE_C = (4, 8, 12, 16, 24, 32, 48)  # register-row classes of libsf_align (sf_walk.cu)
+AFFINE_C = (4, 6, 8, 9, 10, 11, 12, 14, 16, 20, 24, 28, 32, 40, 48)  # register-row classes of libsf_align (sf_walk.cu)
 MYERS_B = (1, 2, 3, 4, 6, 8, 12, 16)
 
 
@@ -269,6 +270,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--plain-pairs", type=int, default=200)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cigar", type=int, default=1, help="c2/c3: traceback + CIGAR (1) or score only (0)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -285,7 +287,7 @@ def main():
     build.build()
     lib = _abi.load()
     torch.cuda.set_device(local)
-    pool, jobs, pairs_list, kind = workload(args.config, args.scale)
+    pool, jobs, pairs_list, kind = workload(args.config, args.scale, bool(args.cigar))
     ctx = B.Context(local)
     plan = B.Plan(ctx, jobs, pool.size)
     plan.upload(pool)
@@ -325,7 +327,7 @@ def main():
     stages = ["pack"] + [f"{b['kind']}-c{b['c']}{'-wide' if b['wide'] else ''}"
                          f"{'-tb' if b['traceback'] else ''}" for b in desc["buckets"]]
     if len(prof[0]) > len(stages):
-        stages.append("walk+compact")
+        stages.append("cigar-compact")
     avg = [statistics.mean(p[i] for p in prof) for i in range(len(prof[0]))]
     top = max(range(1, 1 + len(desc["buckets"])), key=lambda i: avg[i])
     tb = desc["buckets"][top - 1]
@@ -401,6 +403,8 @@ def main():
         for q in range(n):
             if kind == "myers":
                 A.distance(w.pattern(q), w.text(q), A.Mode.Infix)
+            elif not args.cigar:
+                A.affine(w.pattern(q), w.text(q), A.Mode.Global, A.Affine.ONT, int(w.band[q]))
             else:
                 A.affine_cigar(w.pattern(q), w.text(q), A.Mode.Global, A.Affine.ONT,
                                int(w.band[q]))
@@ -422,7 +426,8 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "int32", "data": "synthetic (seeded; error model of sim.rs)",
-                "config": {"workload": GOLD[args.config], "pairs": int(len(jobs)),
+                "config": {"workload": GOLD[args.config if args.cigar or args.config != "c2" else "c2-score"],
+                           "pairs": int(len(jobs)),
                            "cells_per_step": cells, "l2": "flushed (256 MB write) before each step",
                            "parallelism": f"replicas x{ws}", "form": "batched persistent plan, CUDA graph",
                            "buckets": len(desc["buckets"]), "status_nonzero": bad},

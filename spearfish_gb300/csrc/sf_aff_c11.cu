@@ -1,0 +1,9 @@
+// Register-row banded affine kernels with C = 11 cells per lane (bands up to 352 cells).
+#include "sf_affine_impl.cuh"
+
+namespace sfk {
+cudaError_t launch_affine_regs_11(bool tb, bool local, const AffLaunch& a, int grid, int block,
+                                  cudaStream_t s) {
+  return launch_affine_c<11, false>(tb, local, a, grid, block, s);
+}
+}  // namespace sfk

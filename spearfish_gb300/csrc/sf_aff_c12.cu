@@ -2,8 +2,8 @@
 #include "sf_affine_impl.cuh"
 
 namespace sfk {
-cudaError_t launch_affine_regs_12(bool tb, const AffLaunch& a, int grid, int block,
+cudaError_t launch_affine_regs_12(bool tb, bool local, const AffLaunch& a, int grid, int block,
                                   cudaStream_t s) {
-  return launch_affine_c<12, false>(tb, a, grid, block, s);
+  return launch_affine_c<12, false>(tb, local, a, grid, block, s);
 }
 }  // namespace sfk

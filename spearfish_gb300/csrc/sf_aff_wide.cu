@@ -3,8 +3,8 @@
 #include "sf_affine_impl.cuh"
 
 namespace sfk {
-cudaError_t launch_affine_wide(bool tb, const AffLaunch& a, int grid, int block,
+cudaError_t launch_affine_wide(bool tb, bool local, const AffLaunch& a, int grid, int block,
                                cudaStream_t s) {
-  return launch_affine_c<kWideC, true>(tb, a, grid, block, s);
+  return launch_affine_c<kWideC, true>(tb, local, a, grid, block, s);
 }
 }  // namespace sfk

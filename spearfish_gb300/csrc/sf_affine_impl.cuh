@@ -17,9 +17,10 @@
 // The per-row bookkeeping (row maximum, leftmost best cell, X-drop stop, cut maxima) runs
 // after each row, in row order, as the reference does.
 //
-// Traceback: one nibble per cell -- bits 0-1 the source of H (0 diagonal, 1 vertical F,
-// 2 horizontal E), bit 2 "E opened from H' of the cell to the left", bit 3 "F opened from H
-// of the cell above" -- stored per row as 32 lanes x ceil(C/8) words, lane-fastest.
+// Traceback: four decisions per cell -- "F extended" (vs opened from H above), "diagonal
+// lost" (H' came from F), "E extended" (vs opened from H' on the left), "H came from E" --
+// kept as sign bits in bit-plane words (tb_push), stored per row as 32 lanes x 2 words per
+// 16 cells, lane-fastest, and walked into a CIGAR by the same warp (walk_warp).
 #pragma once
 #include <type_traits>
 
@@ -76,8 +77,31 @@ struct Win {
   }
 };
 
+// Traceback words of one lane and row: cells in groups of 16, each group two 32-bit words of
+// two bit-planes pushed MSB-first (see row_chunk).
 template <int C>
-using TbWords = uint32_t[(C + 7) / 8];
+using TbWords = uint32_t[2 * ((C + 15) / 16)];
+
+// The pass's scoring, with `one` an opaque 1: `a * one + b` issues on the FMA pipe (IMAD)
+// instead of the integer ALU pipe, which the maxima keep busy.
+struct Sc {
+  int32_t mat, nmis, go, ext, one;
+};
+
+__device__ __forceinline__ int32_t opaque_one() {
+  int32_t v;
+  asm volatile("mov.b32 %0, 1;" : "=r"(v));
+  return v;
+}
+
+// Traceback bits are the signs of differences, shifted into bit-plane words: for each group
+// of 16 cells of a lane, word A receives per cell (pass 1) "F extended" (ho < fo) then
+// "diagonal lost" (dg < fj), word B (pass 2) "E extended" (xo < ee) then "H from E" (x < e).
+// A push is one funnel shift: acc = (acc << 1) | (diff >> 31).  After a row, cell p of a
+// group of g cells holds its first bit at position 2*(g-1-p)+1 and its second at 2*(g-1-p).
+__device__ __forceinline__ uint32_t tb_push(uint32_t acc, int32_t diff) {
+  return __funnelshift_l((uint32_t)diff, acc, 1);
+}
 
 // Pass 1 + scan + pass 2 for one chunk of cells (offsets Q + lane*C + c).
 //   d        lo_i - lo_{i-1}
@@ -86,104 +110,105 @@ using TbWords = uint32_t[(C + 7) / 8];
 //   e0       horizontal gap entering offset Q (NEG at the band's left end)
 //   xprev0   H' of offset Q - 1 (traceback only)
 // h, f hold the previous row on entry and this row on exit.  ecarry / xlast: what enters
-// the next chunk.
-template <int C, bool TB>
+// the next chunk.  Cells past the band are computed too (garbage); the caller masks what
+// later rows read.
+template <int C, bool TB, bool LOCAL>
 __device__ __forceinline__ void row_chunk(int32_t (&h)[C], int32_t (&f)[C], int d, int32_t nH,
                                           int32_t nF, int32_t pHl, const Win<C>& win,
-                                          uint32_t cpat, int32_t mat, int32_t mis, int32_t go,
-                                          int32_t ext, int32_t floor_, bool col0, bool local,
-                                          int32_t e0, int32_t xprev0, int lane, TbWords<C>& tbw,
-                                          int32_t& ecarry, int32_t& xlast) {
-  constexpr bool KEEP = C <= 16;
-  int32_t el[KEEP ? C : 1];
-  // Traceback: per cell "diagonal >= vertical" and "F opened" (one bit per cell of the lane).
-  using Mask = typename std::conditional<(C > 32), uint64_t, uint32_t>::type;
-  Mask dgb = 0, fob = 0;
+                                          uint32_t cpat, const Sc& sc, int32_t floor_,
+                                          bool col0, int32_t e0, int32_t xprev0, int lane,
+                                          TbWords<C>& tbw, int32_t& ecarry, int32_t& xlast) {
+  constexpr int NW = Win<C>::NW;
+  const int32_t go = sc.go, ext = sc.ext, one = sc.one;
+  // Match bits: bit 2k of eqm[g] is set when text base k of group g equals the row's base.
+  uint32_t eqm[NW];
+  {
+    const uint32_t rep = (cpat & 3u) * 0x55555555u;
+    const bool amb = cpat > 3u;  // local band: a read code of 4+ matches nothing
+#pragma unroll
+    for (int g = 0; g < NW; ++g) {
+      const uint32_t x = win.w[g] ^ rep;
+      eqm[g] = amb ? 0u : (~(x | (x >> 1)) & 0x55555555u);
+    }
+  }
+  constexpr int TG = (C + 15) / 16;
+  if constexpr (TB) {
+#pragma unroll
+    for (int q = 0; q < 2 * TG; ++q) tbw[q] = 0;
+  }
   int32_t chain = NEG_INF;
-  const int32_t nmis = -mis;
+  auto cell = [&](int c, int32_t hd, int32_t hu, int32_t fu, bool first_col) {
+    const int32_t ho = hu * one - go;
+    const int32_t fo = addmax(fu, -ext, NEG);  // max(fu - ext, NEG)
+    const int32_t fj = max(ho, fo);
+    if constexpr (TB) tbw[c >> 4] = tb_push(tbw[c >> 4], ho * one - fo);  // F extended
+    int32_t x;
+    if (first_col) {
+      // Column 0: only a vertical gap reaches it (align.rs:2558-2566; local: 818-825).
+      x = LOCAL ? max(fj, floor_) : fj;
+      if constexpr (TB) tbw[c >> 4] = tb_push(tbw[c >> 4], 0);
+    } else {
+      const int32_t dg = hd * one + (((eqm[c >> 4] >> (2 * (c & 15))) & 1u) ? sc.mat : sc.nmis);
+      x = max(dg, fj);
+      if constexpr (TB) tbw[c >> 4] = tb_push(tbw[c >> 4], dg * one - fj);  // diagonal lost
+      if constexpr (LOCAL) x = max(x, floor_);
+    }
+    chain = addmax(chain, -ext, x * one - go);
+    f[c] = fj;
+    return x;
+  };
   if (d) {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      const int32_t hd = h[c];
       const int32_t hu = c + 1 < C ? h[c + 1] : nH;
       const int32_t fu = c + 1 < C ? f[c + 1] : nF;
-      const int32_t fo = fu - ext, ho = hu - go;
-      const int32_t fj = max3(ho, fo, NEG);
-      const int32_t dg = hd + (win.at(c) == cpat ? mat : nmis);
-      const int32_t x = max3(dg, fj, floor_);
-      if constexpr (TB) {
-        dgb |= (Mask)(dg >= fj) << c;
-        fob |= (Mask)(ho >= fo) << c;
-      }
-      if constexpr (KEEP) el[c] = chain;
-      chain = addmax(chain, -ext, x - go);
-      h[c] = x;
-      f[c] = fj;
+      h[c] = cell(c, h[c], hu, fu, false);
     }
   } else {
     int32_t hd = pHl;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      const int32_t hu = h[c], fu = f[c];
-      const int32_t fo = fu - ext, ho = hu - go;
-      int32_t fj, x;
-      if (c == 0 && col0) {
-        // Column 0: only a vertical gap reaches it (align.rs:2558-2566; local: 818-825).
-        fj = local ? max3(ho, fo, NEG) : max(ho, fo);
-        x = local ? max(fj, floor_) : fj;
-        if constexpr (TB) fob |= (Mask)(ho >= fo);
-      } else {
-        fj = max3(ho, fo, NEG);
-        const int32_t dg = hd + (win.at(c) == cpat ? mat : nmis);
-        x = max3(dg, fj, floor_);
-        if constexpr (TB) {
-          dgb |= (Mask)(dg >= fj) << c;
-          fob |= (Mask)(ho >= fo) << c;
-        }
-      }
-      if constexpr (KEEP) el[c] = chain;
-      chain = addmax(chain, -ext, x - go);
+      const int32_t hu = h[c];
+      h[c] = cell(c, hd, hu, f[c], c == 0 && col0);
       hd = hu;
-      h[c] = x;
-      f[c] = fj;
     }
   }
-  // Gap entering each lane: S_l = max_{l' <= l} chain_l' - ext*C*(l - l').
+  // Gap entering each lane: S_l = max_{l' <= l} chain_l' - ext*C*(l - l').  A low lane's
+  // shuffle returns its own S, which max(S - k, S) leaves unchanged.
   const int32_t dC = ext * C;
   int32_t S = chain;
 #pragma unroll
-  for (int sft = 1; sft < 32; sft <<= 1) {
-    const int32_t tv = __shfl_up_sync(FULL, S, sft);
-    if (lane >= sft) S = addmax(tv, -dC * sft, S);
-  }
+  for (int sft = 1; sft < 32; sft <<= 1)
+    S = addmax(__shfl_up_sync(FULL, S, sft), -dC * sft, S);
   const int32_t Sp = __shfl_up_sync(FULL, S, 1);
   const int32_t ein = lane == 0 ? e0 : addmax(e0, -dC * lane, Sp);
   ecarry = __shfl_sync(FULL, addmax(e0, -dC * 32, S), 31);
-  int32_t xprev = 0;
+  int32_t xp = 0;
   if constexpr (TB) {
     const int32_t xl = __shfl_up_sync(FULL, h[C - 1], 1);
-    xprev = lane == 0 ? xprev0 : xl;
-#pragma unroll
-    for (int q = 0; q < (C + 7) / 8; ++q) tbw[q] = 0;
+    xp = lane == 0 ? xprev0 : xl;
   }
   xlast = __shfl_sync(FULL, h[C - 1], 31);
-  // Pass 2.
-  int32_t e = ein, xp = 0;
+  // Pass 2: E_c = max(H'_{c-1} - go, E_{c-1} - ext), H = max(H', E).
+  int32_t e = ein;
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const int32_t x = h[c];
-    if constexpr (KEEP) {
-      if (c > 0) e = addmax(ein, -ext * c, el[c]);
-    } else {
-      if (c > 0) e = addmax(e, -ext, xp - go);
-      xp = x;
+    const int32_t xo = xp * one - go;  // H'_{c-1} - go (c = 0: the previous lane's last)
+    if (c > 0) {
+      if constexpr (TB) {
+        const int32_t ee = e * one - ext;
+        e = max(xo, ee);
+        tbw[TG + (c >> 4)] = tb_push(tbw[TG + (c >> 4)], xo * one - ee);  // E extended
+      } else {
+        e = addmax(e, -ext, xo);
+      }
+    } else if constexpr (TB) {
+      // ein was formed by the scan: it opened here iff it equals the left cell's H' - go.
+      tbw[TG] = tb_push(tbw[TG], e == xo ? 0 : -1);
     }
-    if constexpr (TB) {
-      const uint32_t hs = e > x ? 2u : (((dgb >> c) & 1u) ? 0u : 1u);
-      const uint32_t eo = (uint32_t)(e == xprev - go);
-      tbw[c >> 3] |= (hs | (eo << 2) | ((uint32_t)((fob >> c) & 1u) << 3)) << (4 * (c & 7));
-      xprev = x;
-    }
+    if constexpr (TB) tbw[TG + (c >> 4)] = tb_push(tbw[TG + (c >> 4)], x * one - e);  // H from E
+    xp = x;
     h[c] = max(x, e);
   }
 }
@@ -213,6 +238,7 @@ __device__ __forceinline__ int32_t lane_max(const int32_t (&h)[C]) {
 template <int C>
 __device__ __forceinline__ int32_t lane_max_below(const int32_t (&h)[C], int64_t base,
                                                   int64_t lim) {
+  // max over cells with offset base + c < lim
   int32_t v = NEG;
 #pragma unroll
   for (int c = 0; c < C; ++c)
@@ -282,75 +308,455 @@ struct Book {
 
 // ---------------------------------------------------------------------------------------
 // Register rows: the band fits 32 * C offsets.
-template <int C, bool TB>
+
+// Row geometry in 32-bit arithmetic (sequences are shorter than 2^30 bases; the host clamps
+// the band reaches to +-2^30).
+struct Geo32 {
+  bool full, local;
+  int32_t below, above, n;
+  __device__ __forceinline__ void range(int32_t i, int32_t& lo, int32_t& hi) const {
+    if (local) {
+      int32_t l = i + below, h = i + above + 1;
+      l = l < 0 ? 0 : (l > n + 1 ? n + 1 : l);
+      h = h < 0 ? 0 : (h > n + 1 ? n + 1 : h);
+      lo = l;
+      hi = (h < l ? l : h) - 1;
+    } else if (full) {
+      lo = 0;
+      hi = n;
+    } else {
+      lo = i > below ? i - below : 0;
+      hi = i + above < n ? i + above : n;
+    }
+  }
+};
+
+__device__ __forceinline__ int32_t clamp30(int64_t v) {
+  const int64_t k = int64_t(1) << 30;
+  return (int32_t)(v < -k ? -k : (v > k ? k : v));
+}
+
+// ---------------------------------------------------------------------------------------
+// Traceback walk (no reference counterpart: spearfish computes no alignment path).  The warp
+// that computed a pass walks it right after, on lane 0: from the end cell back to row 0 /
+// column 0 through the pass's nibbles, with the tie order they encode (H from H' before E,
+// diagonal before vertical, opening before extending), writing the CIGAR run-length encoded,
+// BAM-style (len << 4 | op).  The walk is memory-latency bound while the passes are ALU
+// bound, so the other warps' rows hide it.  Every nibble address is range-checked against
+// the row's band before it is read; a path that leaves the band reports "no path".
+// A cell's decisions from its group's two bit-plane words, as a nibble: bit 0 "H' came from F",
+// bit 1 "H came from E", bit 2 "E opened", bit 3 "F opened".
+template <int C>
+__device__ __forceinline__ uint32_t tb_decode(uint32_t wa, uint32_t wb, int c) {
+  const int g = c >> 4, p = c & 15;
+  const int gs = (C - 16 * g) < 16 ? (C - 16 * g) : 16;
+  const int sh = 2 * (gs - 1 - p);
+  const uint32_t a = (wa >> sh) & 3u, b = (wb >> sh) & 3u;  // (first << 1) | second
+  // a: (F extended, diagonal lost); b: (E extended, H from E)
+  return (a & 1u) | ((b & 1u) << 1) | (((b >> 1) ^ 1u) << 2) | (((a >> 1) ^ 1u) << 3);
+}
+
+struct OpWriter {
+  uint32_t* out;
+  uint32_t cap, n = 0;
+  int status = 0;
+  __device__ void push(uint32_t op, uint32_t len) {
+    if (len == 0 || status) return;
+    if (n > 0 && (out[n - 1] & 15u) == op) {
+      out[n - 1] += len << 4;
+      return;
+    }
+    if (n == cap) {
+      status = -1;
+      return;
+    }
+    out[n++] = (len << 4) | op;
+  }
+};
+
+template <int C, bool WIDE>
+__device__ void walk_pass(const sfk::AffLaunch& a, uint32_t jid, const PassCtx& x, const Geo32& g,
+                          const DRes& R) {
+  constexpr int CW = 2 * ((C + 15) / 16);
+  const TJob T = a.tjobs[jid];
+  const int32_t m = (int32_t)x.m;
+  const uint64_t stride_w =
+      WIDE ? tb_row_words(C, wide_chunks(C, band_wmax(x.J, x.P.flags))) : tb_row_words(C, 1);
+  // End cell (align.rs:2643-2650 score_col; 975-981 the window's choice).
+  int32_t score, ei, ej, tail = 0;
+  bool ok = true;
+  if (T.kind == 0) {
+    score = R.score;
+    ei = m;
+    ej = (int32_t)R.score_col;
+    ok = R.score > NEG / 2;
+  } else {
+    const int32_t whole = sat_add(R.score, T.end_bonus);
+    if (R.clip_best >= whole) {
+      score = R.clip_best;
+      ei = (int32_t)R.clip_i;
+      ej = (int32_t)R.clip_j;
+      tail = m - ei;
+    } else {
+      score = whole;
+      ei = m;
+      ej = (int32_t)R.score_col;
+      ok = R.score > NEG / 2;
+    }
+  }
+  OpWriter w{a.ops + T.ops_off, T.ops_cap};
+  int32_t text_start = 0;
+  if (!ok) {
+    w.status = 1;
+  } else {
+    w.push(4, (uint32_t)tail);
+    int32_t i = ei, j = ej;
+    int state = 0;  // 0 H, 1 E, 2 F
+    const int64_t guard = 2 * ((int64_t)m + x.J.n) + 8;
+    for (int64_t it = 0;; ++it) {
+      if (it > guard) {
+        w.status = 1;
+        break;
+      }
+      if (state == 0 && i == 0) {
+        if (x.mode == 0)
+          text_start = j;
+        else
+          w.push(2, (uint32_t)j);
+        break;
+      }
+      if (state == 0 && j == 0) {
+        w.push(1, (uint32_t)i);
+        break;
+      }
+      if (i <= 0 || j <= 0) {
+        w.status = 1;
+        break;
+      }
+      int32_t lo, hi;
+      g.range(i, lo, hi);
+      const int32_t K = j - lo;
+      if (K < 0 || j > hi) {
+        w.status = 1;
+        break;
+      }
+      uint64_t word;
+      int c;
+      constexpr int TG = (C + 15) / 16;
+      if constexpr (WIDE) {
+        const int32_t qc = K / (32 * C), r = K % (32 * C);
+        c = r % C;
+        word = x.J.tb_word + (uint64_t)(i - 1) * stride_w + (uint64_t)qc * CW * 32 +
+               (uint64_t)(c >> 4) * 32 + (uint64_t)(r / C);
+      } else {
+        c = K % C;
+        word = x.J.tb_word + (uint64_t)(i - 1) * stride_w + (uint64_t)(c >> 4) * 32 +
+               (uint64_t)(K / C);
+      }
+      const uint32_t nib = tb_decode<C>(a.tb[word], a.tb[word + TG * 32], c);
+      if (state == 0) {
+        if (nib & 2u) {
+          state = 1;
+        } else if (!(nib & 1u)) {
+          w.push(0, 1);
+          --i;
+          --j;
+        } else {
+          state = 2;
+        }
+      } else if (state == 1) {
+        w.push(2, 1);
+        state = (nib & 4u) ? 0 : 1;
+        --j;
+      } else {
+        w.push(1, 1);
+        state = (nib & 8u) ? 0 : 2;
+        --i;
+      }
+      if (w.status) break;
+    }
+  }
+  if (w.status == 0) {
+    for (uint32_t p = 0, q = w.n ? w.n - 1 : 0; p < q; ++p, --q) {
+      const uint32_t t = w.out[p];
+      w.out[p] = w.out[q];
+      w.out[q] = t;
+    }
+  }
+  TRes tr;
+  tr.score = score;
+  tr.status = w.status;
+  tr.end_i = (uint32_t)ei;
+  tr.end_j = (uint32_t)ej;
+  tr.text_start = (uint32_t)text_start;
+  tr.n_ops = w.status == 0 ? w.n : 0;
+  a.tres[jid] = tr;
+}
+
+// The same walk by a whole warp, for register rows.  The warp keeps a cache of 32 rows x 3
+// lanes' traceback words: lane q holds row rbase - q, for the band lanes L0 - 1 .. L0 + 1 around
+// the path.  A path moves up one row per diagonal or vertical step and drifts sideways slowly,
+// so one round of 32 parallel loads serves ~32 rows; each step then costs a shuffle, not a
+// dependent memory round trip.  All lanes run the walk in lockstep (the state is uniform);
+// lane 0 writes the CIGAR, run-length merged in registers.
+template <int C>
+__device__ void walk_warp(const sfk::AffLaunch& a, uint32_t jid, const PassCtx& x, const Geo32& g,
+                          const DRes& R, int lane) {
+  constexpr int CW = 2 * ((C + 15) / 16);
+  constexpr int NC = 3 * CW;
+  const TJob T = a.tjobs[jid];
+  const int32_t m = (int32_t)x.m;
+  const uint32_t* tb = a.tb + x.J.tb_word;
+  int32_t score, ei, ej, tail = 0;
+  bool ok = true;
+  if (T.kind == 0) {
+    score = R.score;
+    ei = m;
+    ej = (int32_t)R.score_col;
+    ok = R.score > NEG / 2;
+  } else {
+    const int32_t whole = sat_add(R.score, T.end_bonus);
+    if (R.clip_best >= whole) {
+      score = R.clip_best;
+      ei = (int32_t)R.clip_i;
+      ej = (int32_t)R.clip_j;
+      tail = m - ei;
+    } else {
+      score = whole;
+      ei = m;
+      ej = (int32_t)R.score_col;
+      ok = R.score > NEG / 2;
+    }
+  }
+  uint32_t* out = a.ops + T.ops_off;
+  const uint32_t cap = T.ops_cap;
+  uint32_t n_ops = 0, cur_op = 15, cur_len = 0;
+  int status = ok ? 0 : 1;
+  auto flush = [&]() {
+    if (cur_len == 0) return;
+    if (n_ops == cap) {
+      status = -1;
+      return;
+    }
+    if (lane == 0) out[n_ops] = (cur_len << 4) | cur_op;
+    ++n_ops;
+  };
+  auto push = [&](uint32_t op, uint32_t len) {
+    if (len == 0 || status) return;
+    if (op == cur_op) {
+      cur_len += len;
+      return;
+    }
+    flush();
+    cur_op = op;
+    cur_len = len;
+  };
+  int32_t text_start = 0;
+  if (ok) {
+    push(4, (uint32_t)tail);
+    int32_t i = ei, j = ej;
+    int state = 0;  // 0 H, 1 E, 2 F
+    int32_t rbase = -1, L0 = -100;
+    uint32_t cache[NC];
+    const int64_t guard = 2 * ((int64_t)m + x.J.n) + 8;
+    for (int64_t it = 0; !status; ++it) {
+      if (it > guard) {
+        status = 1;
+        break;
+      }
+      if (state == 0 && i == 0) {
+        if (x.mode == 0)
+          text_start = j;
+        else
+          push(2, (uint32_t)j);
+        break;
+      }
+      if (state == 0 && j == 0) {
+        push(1, (uint32_t)i);
+        break;
+      }
+      if (i <= 0 || j <= 0) {
+        status = 1;
+        break;
+      }
+      int32_t lo, hi;
+      g.range(i, lo, hi);
+      const int32_t K = j - lo;
+      if (K < 0 || j > hi) {
+        status = 1;
+        break;
+      }
+      const int32_t Lk = K / C, c = K % C;
+      if (i > rbase || i < rbase - 31 || Lk < L0 - 1 || Lk > L0 + 1) {
+        // Refill: lane q loads row i - q's words for band lanes Lk - 1 .. Lk + 1.
+        rbase = i;
+        L0 = Lk;
+        const int32_t r = i - lane;
+#pragma unroll
+        for (int dl = 0; dl < 3; ++dl) {
+          const int32_t L = L0 - 1 + dl;
+#pragma unroll
+          for (int w = 0; w < CW; ++w)
+            cache[dl * CW + w] = (r >= 1 && L >= 0 && L < 32)
+                                     ? tb[(uint64_t)(r - 1) * (CW * 32) + w * 32 + L]
+                                     : 0u;
+        }
+      }
+      constexpr int TG = (C + 15) / 16;
+      const int idx = (Lk - L0 + 1) * CW + (c >> 4);
+      uint32_t va = cache[0], vb = cache[TG];
+#pragma unroll
+      for (int q = 1; q < NC; ++q) {
+        if (q == idx) va = cache[q];
+        if (q == idx + TG) vb = cache[q];
+      }
+      const uint32_t wa = __shfl_sync(FULL, va, rbase - i);
+      const uint32_t wb = __shfl_sync(FULL, vb, rbase - i);
+      const uint32_t nib = tb_decode<C>(wa, wb, c);
+      if (state == 0) {
+        if (nib & 2u) {
+          state = 1;
+        } else if (!(nib & 1u)) {
+          push(0, 1);
+          --i;
+          --j;
+        } else {
+          state = 2;
+        }
+      } else if (state == 1) {
+        push(2, 1);
+        state = (nib & 4u) ? 0 : 1;
+        --j;
+      } else {
+        push(1, 1);
+        state = (nib & 8u) ? 0 : 2;
+        --i;
+      }
+    }
+    if (!status) flush();
+  }
+  __syncwarp();
+  if (status == 0) {
+    // Reverse in place, the lanes swapping pairs in parallel.
+    for (uint32_t p = lane; p < n_ops / 2; p += 32) {
+      const uint32_t q = n_ops - 1 - p;
+      const uint32_t t = out[p];
+      out[p] = out[q];
+      out[q] = t;
+    }
+  }
+  if (lane == 0) {
+    TRes tr;
+    tr.score = score;
+    tr.status = status;
+    tr.end_i = (uint32_t)ei;
+    tr.end_j = (uint32_t)ej;
+    tr.text_start = (uint32_t)text_start;
+    tr.n_ops = status == 0 ? n_ops : 0;
+    a.tres[jid] = tr;
+  }
+}
+
+// Sets cell c of the lane to NEG (a jump to the one cell, not a scan over all of them).
+template <int C>
+__device__ __forceinline__ void set_neg(int32_t (&h)[C], int32_t (&f)[C], int c) {
+  switch (c) {
+#define SF_NEG_CASE(k)            \
+  case k:                         \
+    if constexpr (k < C) {        \
+      h[k] = NEG;                 \
+      f[k] = NEG;                 \
+    }                             \
+    break;
+    SF_NEG_CASE(0) SF_NEG_CASE(1) SF_NEG_CASE(2) SF_NEG_CASE(3) SF_NEG_CASE(4) SF_NEG_CASE(5)
+    SF_NEG_CASE(6) SF_NEG_CASE(7) SF_NEG_CASE(8) SF_NEG_CASE(9) SF_NEG_CASE(10) SF_NEG_CASE(11)
+    SF_NEG_CASE(12) SF_NEG_CASE(13) SF_NEG_CASE(14) SF_NEG_CASE(15) SF_NEG_CASE(16)
+    SF_NEG_CASE(17) SF_NEG_CASE(18) SF_NEG_CASE(19) SF_NEG_CASE(20) SF_NEG_CASE(21)
+    SF_NEG_CASE(22) SF_NEG_CASE(23) SF_NEG_CASE(24) SF_NEG_CASE(25) SF_NEG_CASE(26)
+    SF_NEG_CASE(27) SF_NEG_CASE(28) SF_NEG_CASE(29) SF_NEG_CASE(30) SF_NEG_CASE(31)
+    SF_NEG_CASE(32) SF_NEG_CASE(33) SF_NEG_CASE(34) SF_NEG_CASE(35) SF_NEG_CASE(36)
+    SF_NEG_CASE(37) SF_NEG_CASE(38) SF_NEG_CASE(39) SF_NEG_CASE(40) SF_NEG_CASE(41)
+    SF_NEG_CASE(42) SF_NEG_CASE(43) SF_NEG_CASE(44) SF_NEG_CASE(45) SF_NEG_CASE(46)
+    SF_NEG_CASE(47)
+#undef SF_NEG_CASE
+    default:
+      break;
+  }
+  static_assert(C <= 48, "set_neg covers 48 cells per lane");
+}
+
+// The band of a row occupies offsets [0, W); a lane's cells past W hold garbage.  A later row
+// reads the previous row at offsets up to W only (each end of the band moves right by 0 or 1
+// per row), so offset W -- the reference's sentinel right of the band (align.rs:2490-2494)
+// -- is set to NEG and nothing past it is ever read.  Row maxima mask the garbage.
+template <int C, bool TB, bool LOCAL>
 __device__ void pair_regs(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   const PassCtx x = make_ctx(a, jid);
-  constexpr int CW = (C + 7) / 8;
+  const Sc sc{x.mat, -x.mis, x.go, x.ext, opaque_one()};
+  constexpr int CW = 2 * ((C + 15) / 16);
   DRes r{};
-  if (x.local && (x.m == 0 || x.J.below > x.J.above)) {
+  if (LOCAL && (x.m == 0 || x.J.below > x.J.above)) {
     if (lane == 0) {
       r.score = 0;
       a.out[jid] = r;
     }
     return;
   }
+  const int32_t m = (int32_t)x.m, n = (int32_t)x.n;
+  const Geo32 g{(x.P.flags & F_FULL) != 0, LOCAL, clamp30(x.J.below), clamp30(x.J.above), n};
+  const int32_t cut = x.cuton ? (int32_t)(x.J.cut < (uint64_t)n + 1 ? x.J.cut : (uint64_t)n + 1) : INT32_MAX;
+  const int32_t kb = lane * C;  // this lane's first offset
   int32_t h[C], f[C];
-  int64_t plo, phi;
-  x.g.range(0, plo, phi);
+  int32_t plo, phi;
+  g.range(0, plo, phi);
   {
-    const int64_t w0 = phi - plo + 1;
+    const int32_t w0 = phi - plo + 1;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      const int64_t K = (int64_t)lane * C + c;
-      h[c] = K < w0 ? row0_value(x, plo + K) : NEG;
+      h[c] = kb + c < w0 ? row0_value(x, plo + kb + c) : NEG;
       f[c] = NEG;
     }
   }
   Book b;
   bool stopped = false;
   uint32_t pw = 0;
-  for (int64_t i = 1; i <= x.m; ++i) {
-    int64_t lo, hi;
-    x.g.range(i, lo, hi);
-    if (!x.local && lo > hi) {
-      r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)x.n, (uint32_t)i,
+  uint32_t* tbp = TB ? a.tb + x.J.tb_word + lane : nullptr;
+  for (int32_t i = 1; i <= m; ++i) {
+    int32_t lo, hi;
+    g.range(i, lo, hi);
+    if (!LOCAL && lo > hi) {
+      r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)i,
                b.rows, b.cells};
       stopped = true;
       break;
     }
-    const int d = (int)(lo - plo);
-    const int64_t W = hi - lo + 1;
+    const int d = lo - plo;
+    const int32_t W = hi - lo + 1;
     const uint32_t cpat = pattern_code(a, x, i, pw);
-    const int32_t floor_ = x.local ? (i < x.m ? 0 : NEG) : NEG;
+    const int32_t floor_ = LOCAL ? (i < m ? 0 : NEG) : NEG;
     int32_t nH = __shfl_down_sync(FULL, h[0], 1), nF = __shfl_down_sync(FULL, f[0], 1);
     if (lane == 31) nH = nF = NEG;
     const int32_t pHl = __shfl_up_sync(FULL, h[C - 1], 1);
     Win<C> win;
-    win.load(a.pool, x.J.t_word, lo + (int64_t)lane * C);
+    win.load(a.pool, x.J.t_word, lo + kb);
     const bool col0 = lo == 0 && lane == 0 && W > 0;
     int32_t ecarry, xlast;
     TbWords<C> tbw;
-    row_chunk<C, TB>(h, f, d, nH, nF, pHl, win, cpat, x.mat, x.mis, x.go, x.ext, floor_, col0,
-                     x.local, NEG, NEG_INF, lane, tbw, ecarry, xlast);
-    if ((int64_t)lane * C + C > W) {
-#pragma unroll
-      for (int c = 0; c < C; ++c)
-        if ((int64_t)lane * C + c >= W) h[c] = f[c] = NEG;
-    }
+    row_chunk<C, TB, LOCAL>(h, f, d, nH, nF, pHl, win, cpat, sc, floor_, col0, NEG, NEG_INF,
+                            lane, tbw, ecarry, xlast);
+    if (W < 32 * C && lane == W / C) set_neg(h, f, W - kb);
     if constexpr (TB) {
-      uint32_t* dst = a.tb + x.J.tb_word + (uint64_t)(i - 1) * (CW * 32);
 #pragma unroll
-      for (int q = 0; q < CW; ++q) dst[q * 32 + lane] = tbw[q];
+      for (int q = 0; q < CW; ++q) tbp[q * 32] = tbw[q];
+      tbp += CW * 32;
     }
     b.cells += (uint64_t)(W > 0 ? W : 0);
     b.rows += 1;
     if (x.rowmax_on) {
-      const int32_t rmax = __reduce_max_sync(FULL, lane_max(h));
-      if (x.cuton && lo <= (int64_t)x.J.cut) {
+      const int32_t rmax = __reduce_max_sync(FULL, lane_max_below(h, kb, W));
+      if (x.cuton && lo <= cut) {
         int32_t row = rmax;
-        if (hi > (int64_t)x.J.cut)
-          row = __reduce_max_sync(
-              FULL, lane_max_below(h, (int64_t)lane * C, (int64_t)x.J.cut - lo + 1));
+        if (hi > cut) row = __reduce_max_sync(FULL, lane_max_below(h, kb, cut - lo + 1));
         b.cut_best = max(b.cut_best, row);
       }
       if (x.clip) {
@@ -368,42 +774,48 @@ __device__ void pair_regs(const sfk::AffLaunch& a, uint32_t jid, int lane) {
           break;
         }
       }
-      if (x.local) {
+      if (LOCAL) {
         b.best_local = max(b.best_local, rmax);
-        if (i == x.m) b.best_local = max(b.best_local, sat_add(rmax, x.P.bonus1));
+        if (i == m) b.best_local = max(b.best_local, sat_add(rmax, x.P.bonus1));
       }
     }
     plo = lo;
     phi = hi;
   }
   if (!stopped) {
+    const int32_t W = phi - plo + 1;
     r.clip_best = b.clip_best;
     r.cut_best = b.cut_best;
     r.clip_i = b.ci;
     r.clip_j = b.cj;
     r.text_read = (uint32_t)phi;
-    r.last_row = (uint32_t)x.m;
+    r.last_row = (uint32_t)m;
     r.rows = b.rows;
     r.cells = b.cells;
-    if (x.local) {
+    if (LOCAL) {
       r.score = b.best_local;
     } else if (x.mode == 2) {
-      const int64_t K = x.n - plo;
-      const int owner = (int)(K / C), cs = (int)(K % C);
-      r.score = __shfl_sync(FULL, select_c(h, cs), owner & 31);
-      r.score_col = (uint32_t)x.n;
+      const int32_t K = n - plo;
+      r.score = __shfl_sync(FULL, select_c(h, K % C), (K / C) & 31);
+      r.score_col = (uint32_t)n;
     } else {
-      const int32_t rmax = __reduce_max_sync(FULL, lane_max(h));
+      const int32_t rmax = __reduce_max_sync(FULL, lane_max_below(h, kb, W));
       r.score = rmax;
       r.score_col = (uint32_t)(plo + leftmost(h, rmax, lane));
     }
     r.cut_score = NEG;
-    if (x.cuton && plo <= (int64_t)x.J.cut) {
-      const int64_t lim = min(phi, (int64_t)x.J.cut) - plo + 1;
-      r.cut_score = __reduce_max_sync(FULL, lane_max_below(h, (int64_t)lane * C, lim));
+    if (x.cuton && plo <= cut) {
+      const int32_t lim = min(phi, cut) - plo + 1;
+      r.cut_score = __reduce_max_sync(FULL, lane_max_below(h, kb, lim));
     }
   }
   if (lane == 0) a.out[jid] = r;
+  if constexpr (TB) {
+    // __syncwarp orders the lanes' nibble stores before the walk reads them.
+    __syncwarp();
+    walk_warp<C>(a, jid, x, g, r, lane);
+  }
+  __syncwarp();
 }
 
 // ---------------------------------------------------------------------------------------
@@ -416,10 +828,11 @@ __device__ __forceinline__ uint64_t widx(int64_t K) {
   return (uint64_t)(q * 32 * C + (r % C) * 32 + r / C);
 }
 
-template <int C, bool TB>
+template <int C, bool TB, bool LOCAL>
 __device__ void pair_wide(const sfk::AffLaunch& a, uint32_t jid, int lane, int32_t* scr) {
   const PassCtx x = make_ctx(a, jid);
-  constexpr int CW = (C + 7) / 8;
+  const Sc sc{x.mat, -x.mis, x.go, x.ext, opaque_one()};
+  constexpr int CW = 2 * ((C + 15) / 16);
   constexpr int64_t CH = 32 * C;
   DRes r{};
   if (x.local && (x.m == 0 || x.J.below > x.J.above)) {
@@ -496,8 +909,8 @@ __device__ void pair_wide(const sfk::AffLaunch& a, uint32_t jid, int lane, int32
       const bool col0 = lo == 0 && q == 0 && lane == 0 && W > 0;
       int32_t ecarry, xlast;
       TbWords<C> tbw;
-      row_chunk<C, TB>(h, f, d, nH, nF, pHl, win, cpat, x.mat, x.mis, x.go, x.ext, floor_, col0,
-                       x.local, e0, xprev0, lane, tbw, ecarry, xlast);
+      row_chunk<C, TB, LOCAL>(h, f, d, nH, nF, pHl, win, cpat, sc, floor_, col0, e0, xprev0,
+                              lane, tbw, ecarry, xlast);
       e0 = ecarry;
       xprev0 = xlast;
       const int64_t kb = Q + (int64_t)lane * C;
@@ -599,12 +1012,30 @@ __device__ void pair_wide(const sfk::AffLaunch& a, uint32_t jid, int lane, int32
     }
     r.cut_score = (x.cuton && plo <= (int64_t)x.J.cut) ? cutm : NEG;
   }
-  if (lane == 0) a.out[jid] = r;
+  __syncwarp();
+  if (lane == 0) {
+    a.out[jid] = r;
+    if constexpr (TB) {
+      const Geo32 g32{(x.P.flags & F_FULL) != 0, LOCAL, clamp30(x.J.below), clamp30(x.J.above),
+                      (int32_t)x.n};
+      walk_pass<C, true>(a, jid, x, g32, r);
+    }
+  }
+  __syncwarp();
 }
 
 // One warp per pass; warps take passes from the bucket's queue, longest first.
-template <int C, bool WIDE, bool TB>
-__global__ void __launch_bounds__(128) affine_kernel(sfk::AffLaunch a) {
+// Blocks per SM the register budget aims at: rows of up to 12 cells per lane fit in ~80
+// registers (6 blocks of 4 warps), 16 in ~100; wider rows and the wide-row kernel take what
+// they need.
+template <int C, bool WIDE>
+struct MinBlocks {
+  static constexpr int value =
+      WIDE ? 3 : (C <= 12 ? 6 : (C <= 16 ? 5 : (C <= 20 ? 4 : (C <= 32 ? 3 : 2))));
+};
+
+template <int C, bool WIDE, bool TB, bool LOCAL>
+__global__ void __launch_bounds__(128, MinBlocks<C, WIDE>::value) affine_kernel(sfk::AffLaunch a) {
   const int lane = threadIdx.x & 31;
   const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int32_t* scr = WIDE ? a.scratch + gw * 4 * a.scratch_cells : nullptr;
@@ -615,9 +1046,9 @@ __global__ void __launch_bounds__(128) affine_kernel(sfk::AffLaunch a) {
     if (q >= a.njobs) break;
     const uint32_t jid = a.order[q];
     if constexpr (WIDE)
-      pair_wide<C, TB>(a, jid, lane, scr);
+      pair_wide<C, TB, LOCAL>(a, jid, lane, scr);
     else
-      pair_regs<C, TB>(a, jid, lane);
+      pair_regs<C, TB, LOCAL>(a, jid, lane);
   }
 }
 
@@ -626,11 +1057,14 @@ __global__ void __launch_bounds__(128) affine_kernel(sfk::AffLaunch a) {
 namespace sfk {
 
 template <int C, bool WIDE>
-cudaError_t launch_affine_c(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {
-  if (tb)
-    affine_kernel<C, WIDE, true><<<grid, block, 0, s>>>(a);
+cudaError_t launch_affine_c(bool tb, bool local, const AffLaunch& a, int grid, int block,
+                            cudaStream_t s) {
+  if (local)
+    affine_kernel<C, WIDE, false, true><<<grid, block, 0, s>>>(a);
+  else if (tb)
+    affine_kernel<C, WIDE, true, false><<<grid, block, 0, s>>>(a);
   else
-    affine_kernel<C, WIDE, false><<<grid, block, 0, s>>>(a);
+    affine_kernel<C, WIDE, false, false><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

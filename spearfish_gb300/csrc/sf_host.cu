@@ -389,7 +389,7 @@ int plan_build(sf_plan* P) {
     }
     P->slot[q] = (uint32_t)dj.size();
     const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
-    items.push_back({Key2{p.kind == PK_LOCAL ? PK_AFFINE : PK_AFFINE, c, wide, tb, 32},
+    items.push_back({Key2{p.kind == PK_LOCAL ? PK_LOCAL : PK_AFFINE, c, wide, tb, 32},
                      Item{(uint32_t)dj.size(), work}});
     dj.push_back(j);
     dp.push_back(pr);
@@ -520,7 +520,7 @@ int plan_build(sf_plan* P) {
     std::snprintf(buf, sizeof buf,
                   "%s{\"kind\": \"%s\", \"c\": %d, \"wide\": %s, \"traceback\": %s, \"lanes\": %d, "
                   "\"jobs\": %u, \"grid\": %d, \"block\": %d, \"work\": %llu}",
-                  q ? ", " : "", b.kind == PK_MYERS ? "myers" : "affine", b.c,
+                  q ? ", " : "", b.kind == PK_MYERS ? "myers" : (b.kind == PK_LOCAL ? "local" : "affine"), b.c,
                   b.wide ? "true" : "false", b.tb ? "true" : "false", b.lanes, b.count, b.grid,
                   b.block, (unsigned long long)bwork[q]);
     d += buf;
@@ -596,7 +596,10 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
       al.tb = P->d_tb.as<uint32_t>();
       al.scratch = P->d_scratch.as<int32_t>() + b.scratch_off;
       al.scratch_cells = P->scratch_cells;
-      CK(sfk::launch_affine(b.c, b.wide, b.tb, al, b.grid, b.block, bs));
+      al.tjobs = P->d_tjobs.as<TJob>();
+      al.ops = P->d_ops.as<uint32_t>();
+      al.tres = P->d_tres.as<TRes>();
+      CK(sfk::launch_affine(b.c, b.wide, b.tb, b.kind == PK_LOCAL, al, b.grid, b.block, bs));
     }
     launches++;
     if ((mrc = mark())) return mrc;
@@ -608,23 +611,11 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
     }
   }
   if (P->n_walk) {
-    sfk::WalkLaunch wl;
-    wl.jobs = P->d_djobs.as<DJob>();
-    wl.params = P->d_params.as<DParams>();
-    wl.res = P->d_res.as<DRes>();
-    wl.tjobs = P->d_tjobs.as<TJob>();
-    wl.list = P->d_wlist.as<uint32_t>();
-    wl.cls = P->d_cls.as<uint8_t>();
-    wl.nlist = P->n_walk;
-    wl.pool = P->d_pool.as<uint32_t>();
-    wl.tb = P->d_tb.as<uint32_t>();
-    wl.ops = P->d_ops.as<uint32_t>();
-    wl.tres = P->d_tres.as<TRes>();
-    CK(sfk::launch_walk(wl, s));
+    // The passes walked their own paths (fused into the affine kernels); compact the CIGARs.
     CK(sfk::launch_compact(P->d_tres.as<TRes>(), P->d_tjobs.as<TJob>(), P->d_wlist.as<uint32_t>(),
                            P->n_walk, P->d_offs.as<uint64_t>(), P->d_ops.as<uint32_t>(),
                            P->d_opsc.as<uint32_t>(), P->d_total.as<uint64_t>(), s));
-    launches += 3;
+    launches += 2;
   }
   if ((mrc = mark())) return mrc;
   P->launches = launches;
@@ -847,7 +838,7 @@ extern "C" {
 const char* sf_last_error(void) { return g_err.c_str(); }
 
 const char* sf_version(void) {
-  return "spearfish_gb300 sf_align 0.1 (sm_103a; affine C={4,8,12,16,24,32,48}+wide; "
+  return "spearfish_gb300 sf_align 0.1 (sm_103a; affine C={4,6,8,9,10,11,12,14,16,20,24,28,32,40,48}+wide; "
          "myers B={1,2,3,4,6,8,12,16})";
 }
 

@@ -76,7 +76,8 @@ struct TRes {
   uint32_t end_i, end_j, text_start, n_ops;
 };
 
-__host__ __device__ inline uint32_t tb_words_per_lane(int c) { return (uint32_t)((c + 7) / 8); }
+// Traceback words per lane and row: two bit-plane words per group of 16 cells.
+__host__ __device__ inline uint32_t tb_words_per_lane(int c) { return (uint32_t)(2 * ((c + 15) / 16)); }
 
 // The widest row of a pass: banded rows are at most below + above + 1 cells
 // (align.rs:2458-2468), local rows at most dhi - dlo + 1 (align.rs:800-805), and no row has
@@ -93,7 +94,7 @@ __host__ __device__ inline int64_t band_wmax(const DJob& J, uint32_t flags) {
   return w < 0 ? 0 : (w > n + 1 ? n + 1 : w);
 }
 
-// Traceback words of one row: `chunks` chunks of 32 lanes x ceil(C/8) words.
+// Traceback words of one row: `chunks` chunks of 32 lanes x tb_words_per_lane(C) words.
 __host__ __device__ inline uint64_t tb_row_words(int c, int64_t chunks) {
   return (uint64_t)chunks * 32u * tb_words_per_lane(c);
 }
@@ -141,30 +142,19 @@ struct AffLaunch {
   uint32_t* tb;               // traceback arena
   int32_t* scratch;           // WIDE rows: per warp 4 * scratch_cells int32
   uint64_t scratch_cells;
+  const sf::TJob* tjobs;      // traceback: end cell kind and CIGAR slot per job
+  uint32_t* ops;              // CIGAR slots
+  sf::TRes* tres;             // walk results
 };
 
 // C: cells per lane (register rows); wide: rows in global scratch, chunked.
-cudaError_t launch_affine(int c, bool wide, bool tb, const AffLaunch& a, int grid, int block,
-                          cudaStream_t s);
+cudaError_t launch_affine(int c, bool wide, bool tb, bool local, const AffLaunch& a, int grid,
+                          int block, cudaStream_t s);
 // The C values the register kernel is built for (ascending), and the wide chunk C.
 extern const int kAffineC[];
 extern const int kAffineNC;
 constexpr int kWideC = 16;
 
-struct WalkLaunch {
-  const sf::DJob* jobs;
-  const sf::DParams* params;
-  const sf::DRes* res;
-  const sf::TJob* tjobs;
-  const uint32_t* list;   // jobs that want a CIGAR
-  const uint8_t* cls;     // per job: C value of the kernel that ran it, 0xff for wide
-  uint32_t nlist;
-  const uint32_t* pool;
-  const uint32_t* tb;
-  uint32_t* ops;
-  sf::TRes* tres;
-};
-cudaError_t launch_walk(const WalkLaunch& a, cudaStream_t s);
 
 struct MyersLaunch {
   const sf::MJob* jobs;
