@@ -274,6 +274,28 @@ int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                  sf_result_t *results, uint32_t *ops, uint64_t ops_cap,
                  uint64_t *ops_used);
 
+/* ---- without device allocation ------------------------------------------
+ * No counterpart in the reference: `affine` (align.rs:699-701) for callers
+ * that must not allocate device memory -- a latency-bound serving path, where
+ * cudaMalloc and cudaFree synchronize the device and stall every request in
+ * flight, or an application that hands this library device memory from its
+ * own pool and forbids any other device allocation.  Inputs (byte codes) and
+ * the output score are the caller's device buffers; everything else lives in
+ * one file-scope device array of SF_NOALLOC_SCRATCH bytes per GPU, which
+ * every call shares and which keeps the last call's contents.  Work is queued
+ * on `stream` (a cudaStream_t; NULL for the default stream) and the score is
+ * in *d_score once the stream reaches it.  Pattern and text are limited to
+ * SF_NOALLOC_MAX_LEN bases each (SF_ERR_TOO_LONG beyond).  Calls whose work
+ * overlaps on one GPU race on the array: order them (one stream).  The first
+ * call on a device looks the array up with that device current; make it
+ * before any stream capture. */
+#define SF_NOALLOC_SCRATCH (1u << 19)
+#define SF_NOALLOC_MAX_LEN 16384u
+int sf_affine_noalloc(const uint8_t *d_pattern, uint64_t m,
+                      const uint8_t *d_text, uint64_t n, int mode,
+                      const sf_affine_t *sc, uint64_t band, int32_t *d_score,
+                      void *stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 /* Measured int32 throughput of `device` (tera-ops/s) on the DP kernels'

@@ -114,6 +114,8 @@ SIGNATURES = {
     "sf_plan_launches": (C.c_uint64, [_vp]),
     "sf_plan_describe": (C.c_char_p, [_vp]),
     "sf_plan_profile": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_uint32, _u32p]),
+    "sf_affine_noalloc": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int, _aff,
+                                    C.c_uint64, C.c_void_p, C.c_void_p]),
     "sf_int_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "sf_batch_run": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(JobT), C.c_uint64, _aff,
                                C.c_uint32, C.POINTER(ResultT), _u32p, C.c_uint64, _u64p]),

@@ -831,6 +831,8 @@ Pass affine_pass(uint64_t p_off, uint64_t m, uint64_t t_off, uint64_t n, int mod
 
 }  // namespace
 
+int sf_internal_set_error(int code, const char* msg) { return fail(code, msg); }
+
 // ---- C ABI ------------------------------------------------------------------------------
 
 extern "C" {

@@ -192,3 +192,6 @@ namespace sfk {
 // Runs grid = sms * 8 blocks of 256 threads; returns the elapsed ms and the ops counted.
 cudaError_t run_int_peak(int sms, int32_t* out, float* ms, uint64_t* ops);
 }  // namespace sfk
+
+// Records `msg` as the calling thread's sf_last_error() and returns `code`.
+int sf_internal_set_error(int code, const char* msg);
