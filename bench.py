@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 GOLD = {"c1": "myers-infix-10k", "c2": "affine-global-band128-cigar-20k",
+        "c5": "serving-poisson-2000rps-bursts5x",
         "c2-score": "affine-global-band128-score-20k",
         "c3": "uneven-myers+affine-100k"}
 OPS_PER_CELL = {"affine_tb": 12, "affine": 10, "myers": 0.625}
@@ -257,13 +258,97 @@ def run_reference(args, ws, rank):
     print(json.dumps(line))
 
 
+def pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if xs else None
+
+
+def run_serving(args, ws, rank, local):
+    """Config 5: a bursty Poisson stream of read batches through the serving loop."""
+    import threading
+
+    from spearfish_gb300 import batch as B, build
+    from spearfish_gb300 import serve as S
+    from spearfish_gb300 import workloads as W
+
+    build.build()
+    stream = W.serving_stream(args.serve_seconds, seed=5 + rank)
+    rng = np.random.default_rng(505 + rank)
+    batches = []
+    for _, size in stream:
+        reads = [W.serving_read(rng, hifi=rng.random() < 0.1) for _ in range(size)]
+        batches.append(W.serving_jobs(reads, B))
+    srv = S.Server(local, slots=args.slots)
+    try:
+        for pool, jobs in batches[:3]:  # warm-up: buffers grow to a working size
+            srv.wait(srv.submit(pool, jobs))
+        # Real time: each batch is submitted at its arrival time.
+        tickets = [None] * len(batches)
+        t0 = time.perf_counter()
+
+        def feeder():
+            for q, ((at, _), (pool, jobs)) in enumerate(zip(stream, batches)):
+                d = at - (time.perf_counter() - t0)
+                if d > 0:
+                    time.sleep(d)
+                tickets[q] = srv.submit(pool, jobs)
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        lat, cells, t_last = [], 0, t0
+        for q in range(len(batches)):
+            while tickets[q] is None:
+                time.sleep(0.0002)
+            out, st = srv.wait(tickets[q])
+            lat.append(st.total_ms)
+            cells += st.cells
+            t_last = time.perf_counter()
+        th.join()
+        wall = t_last - t0
+        reads = sum(n for _, n in stream)
+        live = {"p50_ms": pct(lat, 50), "p95_ms": pct(lat, 95), "p99_ms": pct(lat, 99),
+                "max_ms": max(lat), "batches": len(batches), "reads": reads,
+                "offered_reads_per_s": reads / args.serve_seconds,
+                "sustained_gcups": cells / wall / 1e9, "wall_s": wall}
+        # Saturation: every batch submitted at once.
+        t1 = time.perf_counter()
+        tks = [srv.submit(p, j) for p, j in batches]
+        lat2, cells2 = [], 0
+        for t in tks:
+            _, st = srv.wait(t)
+            lat2.append(st.total_ms)
+            cells2 += st.cells
+        wall2 = time.perf_counter() - t1
+        sat = {"p50_ms": pct(lat2, 50), "p99_ms": pct(lat2, 99), "gcups": cells2 / wall2 / 1e9,
+               "wall_s": wall2, "reads_per_s": reads / wall2}
+        q = srv.query()
+    finally:
+        srv.close()
+    if rank == 0:
+        line = {"metric": "alignment GCUPS", "value": sat["gcups"], "unit": "GCUPS",
+                "n_gpus": ws, "steps": 1, "warmup": 3, "ms_per_step": wall2 * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "int32", "data": "synthetic (seeded read model; sim.rs error model)",
+                "config": {"workload": GOLD["c5"], "serve_seconds": args.serve_seconds,
+                           "slots": args.slots, "jobs_per_read": 4,
+                           "parallelism": f"replicas x{ws}"},
+                "latency": live, "saturation": sat,
+                "server": {k: int(v) for k, v in q.items()},
+                "e2e": {"value": sat["gcups"], "unit": "GCUPS",
+                        "h2d_bytes_per_step": int(sum(p.size + j.nbytes for p, j in batches)),
+                        "d2h_bytes_per_step": int(sum(len(j) * 64 for _, j in batches)),
+                        "call": "sf_server_submit / sf_server_wait (C ABI)"}}
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
+    ap.add_argument("--serve-seconds", type=float, default=20.0, help="c5: stream length")
+    ap.add_argument("--slots", type=int, default=8, help="c5: requests on the device at once")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload's pairs")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
@@ -275,6 +360,9 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.config == "c5":
+        run_serving(args, ws, rank, local)
         return
     dist = dist_init(ws)
 

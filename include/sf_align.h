@@ -274,6 +274,49 @@ int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                  sf_result_t *results, uint32_t *ops, uint64_t ops_cap,
                  uint64_t *ops_used);
 
+/* ---- serving: continuous batching ---------------------------------------
+ * Requests (the jobs of a read batch over a byte pool the caller keeps alive
+ * until it waits for them) are admitted in arrival order as soon as a slot
+ * is free and the device memory they need fits the HBM budget; requests on
+ * different slots run on the device at the same time.  A request's results
+ * are the same alone as in any mix. */
+typedef struct sf_server sf_server;
+
+typedef struct {
+    int device;
+    uint32_t slots;       /* requests on the device at once (0: 8) */
+    uint64_t hbm_budget;  /* bytes the slots may hold (0: 90% of free memory) */
+    const sf_affine_t *scores; /* scoring table for sc_index (NULL: ONT) */
+    uint32_t n_scores;
+} sf_server_opts;
+
+typedef struct {
+    double queue_ms;  /* submitted -> admitted to a slot */
+    double run_ms;    /* admitted -> results on the host */
+    double total_ms;  /* submitted -> results on the host */
+    uint64_t cells;   /* DP cells of the request */
+    uint32_t slot;
+    int32_t status;
+} sf_request_stats;
+
+typedef struct {
+    uint64_t submitted, completed, failed, cells;
+    uint64_t hbm_budget, hbm_held;
+    uint32_t slots, busy_slots, pending, pad_;
+} sf_server_stats;
+
+int sf_server_create(const sf_server_opts *opts, sf_server **out);
+/* Stops the loop; requests not yet waited for are dropped. */
+void sf_server_destroy(sf_server *srv);
+int sf_server_submit(sf_server *srv, const uint8_t *pool, uint64_t pool_bytes,
+                     const sf_job_t *jobs, uint64_t count, uint64_t *ticket);
+/* Waits at most timeout_ms (SF_ERR_TIMEOUT; the request stays pending), then
+ * copies the request's results and compacted CIGAR ops and releases it. */
+int sf_server_wait(sf_server *srv, uint64_t ticket, int32_t timeout_ms,
+                   sf_result_t *results, uint32_t *ops, uint64_t ops_cap,
+                   uint64_t *ops_used, sf_request_stats *stats);
+int sf_server_query(sf_server *srv, sf_server_stats *out);
+
 /* ---- without device allocation ------------------------------------------
  * No counterpart in the reference: `affine` (align.rs:699-701) for callers
  * that must not allocate device memory -- a latency-bound serving path, where

@@ -59,6 +59,23 @@ class ResultT(C.Structure):
                 ("status", C.c_int32)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_uint32), ("hbm_budget", C.c_uint64),
+                ("scores", C.POINTER(Affine)), ("n_scores", C.c_uint32)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
+                ("cells", C.c_uint64), ("slot", C.c_uint32), ("status", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cells", C.c_uint64), ("hbm_budget", C.c_uint64), ("hbm_held", C.c_uint64),
+                ("slots", C.c_uint32), ("busy_slots", C.c_uint32), ("pending", C.c_uint32),
+                ("pad_", C.c_uint32)]
+
+
 # Every symbol include/sf_align.h declares, with (restype, argtypes).
 _u8p = C.POINTER(C.c_uint8)
 _u8pp = C.POINTER(_u8p)
@@ -114,6 +131,12 @@ SIGNATURES = {
     "sf_plan_launches": (C.c_uint64, [_vp]),
     "sf_plan_describe": (C.c_char_p, [_vp]),
     "sf_plan_profile": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_uint32, _u32p]),
+    "sf_server_create": (C.c_int, [C.POINTER(ServerOpts), C.POINTER(_vp)]),
+    "sf_server_destroy": (None, [_vp]),
+    "sf_server_submit": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(JobT), C.c_uint64, _u64p]),
+    "sf_server_wait": (C.c_int, [_vp, C.c_uint64, C.c_int32, C.POINTER(ResultT), _u32p,
+                                 C.c_uint64, _u64p, C.POINTER(RequestStats)]),
+    "sf_server_query": (C.c_int, [_vp, C.POINTER(ServerStats)]),
     "sf_affine_noalloc": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int, _aff,
                                     C.c_uint64, C.c_void_p, C.c_void_p]),
     "sf_int_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -1,0 +1,205 @@
+// Internal engine of libsf_align: buffers, passes, plans and contexts shared by the C ABI
+// (sf_host.cu) and the serving loop (sf_server.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sf_align.h"
+#include "sf_internal.cuh"
+
+namespace sfe {
+
+using namespace sf;
+
+// Records the calling thread's sf_last_error() message and returns `code`.
+int fail(int code, const std::string& msg);
+// The calling thread's last message.
+const std::string& last_error();
+
+#define CK(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(e_ == cudaErrorMemoryAllocation ? SF_ERR_NOMEM : SF_ERR_CUDA,     \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
+  } while (0)
+
+inline uint64_t usat_add(uint64_t a, uint64_t b) { return a > UINT64_MAX - b ? UINT64_MAX : a + b; }
+inline uint64_t usat_sub(uint64_t a, uint64_t b) { return a > b ? a - b : 0; }
+inline int32_t sat_add32(int32_t a, int32_t b) {
+  int64_t s = (int64_t)a + b;
+  return s > INT32_MAX ? INT32_MAX : s < INT32_MIN ? INT32_MIN : (int32_t)s;
+}
+constexpr int64_t kGeoCap = int64_t(1) << 40;  // band geometry beyond any text length
+
+// ---- device and pinned buffers ---------------------------------------------------------
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int ensure(size_t n) {
+    if (n <= cap) return SF_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      return fail(SF_ERR_NOMEM, "cudaMalloc(" + std::to_string(want) + "): " + cudaGetErrorString(e));
+    }
+    cap = want;
+    return SF_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct PinBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~PinBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  int ensure(size_t n) {
+    if (n <= cap) return SF_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 256;
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      return fail(SF_ERR_NOMEM, "cudaMallocHost: " + std::string(cudaGetErrorString(e)));
+    }
+    cap = want;
+    return SF_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// ---- passes ----------------------------------------------------------------------------
+
+enum PassKind : uint8_t { PK_MYERS = 0, PK_AFFINE = 1, PK_LOCAL = 2 };
+
+// One DP pass as the reference's `affine_dp` / `distance` / `local_band_core` receive it.
+struct Pass {
+  PassKind kind;
+  uint8_t mode = 0;
+  bool clip = false, cell = false, want_cigar = false;
+  uint8_t tb_kind = 0;  // 0: affine end, 1: extend-window end
+  uint64_t p_off = 0, t_off = 0;  // byte offsets in the pool
+  uint32_t m = 0, n = 0;
+  uint64_t band = SF_NOLIMIT, geom = 0, cut = SF_NOLIMIT;
+  int32_t xdrop = 0, end_bonus = 0, bonus0 = 0, bonus1 = 0;
+  int64_t dlo = 0, dhi = 0;
+  uint32_t k = SF_NONE;
+  sf_affine_t sc{2, 4, 4, 2};
+};
+
+struct Bucket {
+  PassKind kind;
+  int c = 0;       // affine: cells per lane; Myers: blocks per lane
+  bool wide = false, tb = false;
+  int lanes = 32;  // Myers: lanes per pair
+  uint32_t first = 0, count = 0;  // range in the order array
+  int grid = 0, block = 128;
+  uint64_t scratch_off = 0;       // wide rows: this bucket's slice of the scratch (int32s)
+};
+
+}  // namespace sfe
+
+struct sf_plan {
+  using Pass = sfe::Pass;
+  using Bucket = sfe::Bucket;
+  using DevBuf = sfe::DevBuf;
+  using PinBuf = sfe::PinBuf;
+  sf_context* ctx = nullptr;
+  bool owns_ctx = false;
+  std::vector<Pass> passes;
+  // Sequences: unique (byte offset, length), packed word offsets.
+  std::vector<uint64_t> seq_boff, seq_woff;
+  std::vector<uint32_t> seq_len;
+  uint64_t pool_bytes = 0, pool_words = 0;
+  // Per pass: index in its kind's device arrays.
+  std::vector<uint32_t> slot;
+  uint32_t n_aff = 0, n_my = 0, n_walk = 0;
+  std::vector<Bucket> buckets;
+  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
+  int wide_warps = 0;
+  std::string desc;
+  // Device buffers.
+  DevBuf d_bytes, d_pool, d_seq, d_djobs, d_params, d_res, d_mjobs, d_mout, d_tjobs, d_tres,
+      d_tb, d_ops, d_opsc, d_offs, d_order, d_counters, d_wlist, d_cls, d_scratch, d_total;
+  // Pinned staging.
+  PinBuf h_stage, h_res, h_mout, h_tres, h_ops;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_tried = false;
+  uint64_t launches = 0;
+  ~sf_plan() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (owns_ctx) delete ctx;
+  }
+};
+
+// ---- context ---------------------------------------------------------------------------
+
+struct sf_context {
+  int dev = 0;
+  int sms = 0;
+  cudaStream_t s = nullptr;
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork = nullptr, join[kAux] = {};
+  std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
+  ~sf_context() {
+    cache.reset();
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(dev);
+    for (int i = 0; i < kAux; ++i) {
+      if (aux[i]) cudaStreamDestroy(aux[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (s) cudaStreamDestroy(s);
+    cudaSetDevice(prev);
+  }
+};
+
+
+namespace sfe {
+
+int make_context(int device, sf_context** out);
+int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
+                   uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps);
+// Descriptors, buckets and device buffers for P->passes (pool not yet uploaded).
+int plan_build(sf_plan* P);
+int plan_upload_from(sf_plan* P, const uint8_t* pool);
+int plan_execute(sf_plan* P, bool use_graph);
+int plan_fetch(sf_plan* P);
+int plan_fetch_ops(sf_plan* P, uint64_t& total);
+// Converts a fetched plan's results to sf_result_t (and copies compacted ops).
+int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
+                 uint64_t total);
+// Device bytes a plan of these passes needs (upper bound, before building it).
+uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_bytes);
+// Device bytes the plan's buffers hold now.
+uint64_t plan_bytes_held(const sf_plan* P);
+
+}  // namespace sfe

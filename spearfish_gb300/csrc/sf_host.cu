@@ -11,12 +11,9 @@
 #include <tuple>
 #include <vector>
 
-#include "../../include/sf_align.h"
-#include "sf_internal.cuh"
+#include "sf_engine.h"
 
-namespace {
-
-using namespace sf;
+namespace sfe {
 
 thread_local std::string g_err;
 thread_local uint64_t g_dp_cells = 0, g_dp_rows = 0;
@@ -26,168 +23,13 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-#define CK(call)                                                                    \
-  do {                                                                              \
-    cudaError_t e_ = (call);                                                        \
-    if (e_ != cudaSuccess)                                                          \
-      return fail(e_ == cudaErrorMemoryAllocation ? SF_ERR_NOMEM : SF_ERR_CUDA,     \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
-  } while (0)
+const std::string& last_error() { return g_err; }
 
-inline uint64_t usat_add(uint64_t a, uint64_t b) { return a > UINT64_MAX - b ? UINT64_MAX : a + b; }
-inline uint64_t usat_sub(uint64_t a, uint64_t b) { return a > b ? a - b : 0; }
-inline int32_t sat_add32(int32_t a, int32_t b) {
-  int64_t s = (int64_t)a + b;
-  return s > INT32_MAX ? INT32_MAX : s < INT32_MIN ? INT32_MIN : (int32_t)s;
-}
-constexpr int64_t kGeoCap = int64_t(1) << 40;  // band geometry beyond any text length
+}  // namespace sfe
 
-// ---- device and pinned buffers ---------------------------------------------------------
+using namespace sfe;
 
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  int ensure(size_t n) {
-    if (n <= cap) return SF_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = n + n / 4 + 256;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      (void)cudaGetLastError();
-      return fail(SF_ERR_NOMEM, "cudaMalloc(" + std::to_string(want) + "): " + cudaGetErrorString(e));
-    }
-    cap = want;
-    return SF_OK;
-  }
-  template <class T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
-
-struct PinBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  ~PinBuf() {
-    if (p) cudaFreeHost(p);
-  }
-  int ensure(size_t n) {
-    if (n <= cap) return SF_OK;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = n + n / 4 + 256;
-    cudaError_t e = cudaMallocHost(&p, want);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      (void)cudaGetLastError();
-      return fail(SF_ERR_NOMEM, "cudaMallocHost: " + std::string(cudaGetErrorString(e)));
-    }
-    cap = want;
-    return SF_OK;
-  }
-  template <class T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
-
-}  // namespace
-
-namespace {
-
-// ---- passes ----------------------------------------------------------------------------
-
-enum PassKind : uint8_t { PK_MYERS = 0, PK_AFFINE = 1, PK_LOCAL = 2 };
-
-// One DP pass as the reference's `affine_dp` / `distance` / `local_band_core` receive it.
-struct Pass {
-  PassKind kind;
-  uint8_t mode = 0;
-  bool clip = false, cell = false, want_cigar = false;
-  uint8_t tb_kind = 0;  // 0: affine end, 1: extend-window end
-  uint64_t p_off = 0, t_off = 0;  // byte offsets in the pool
-  uint32_t m = 0, n = 0;
-  uint64_t band = SF_NOLIMIT, geom = 0, cut = SF_NOLIMIT;
-  int32_t xdrop = 0, end_bonus = 0, bonus0 = 0, bonus1 = 0;
-  int64_t dlo = 0, dhi = 0;
-  uint32_t k = SF_NONE;
-  sf_affine_t sc{2, 4, 4, 2};
-};
-
-struct Bucket {
-  PassKind kind;
-  int c = 0;       // affine: cells per lane; Myers: blocks per lane
-  bool wide = false, tb = false;
-  int lanes = 32;  // Myers: lanes per pair
-  uint32_t first = 0, count = 0;  // range in the order array
-  int grid = 0, block = 128;
-  uint64_t scratch_off = 0;       // wide rows: this bucket's slice of the scratch (int32s)
-};
-
-}  // namespace
-
-struct sf_plan {
-  sf_context* ctx = nullptr;
-  bool owns_ctx = false;
-  std::vector<Pass> passes;
-  // Sequences: unique (byte offset, length), packed word offsets.
-  std::vector<uint64_t> seq_boff, seq_woff;
-  std::vector<uint32_t> seq_len;
-  uint64_t pool_bytes = 0, pool_words = 0;
-  // Per pass: index in its kind's device arrays.
-  std::vector<uint32_t> slot;
-  uint32_t n_aff = 0, n_my = 0, n_walk = 0;
-  std::vector<Bucket> buckets;
-  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
-  int wide_warps = 0;
-  std::string desc;
-  // Device buffers.
-  DevBuf d_bytes, d_pool, d_seq, d_djobs, d_params, d_res, d_mjobs, d_mout, d_tjobs, d_tres,
-      d_tb, d_ops, d_opsc, d_offs, d_order, d_counters, d_wlist, d_cls, d_scratch, d_total;
-  // Pinned staging.
-  PinBuf h_stage, h_res, h_mout, h_tres, h_ops;
-  cudaGraphExec_t graph = nullptr;
-  bool graph_tried = false;
-  uint64_t launches = 0;
-  ~sf_plan() {
-    if (graph) cudaGraphExecDestroy(graph);
-    if (owns_ctx) delete ctx;
-  }
-};
-
-// ---- context ---------------------------------------------------------------------------
-
-struct sf_context {
-  int dev = 0;
-  int sms = 0;
-  cudaStream_t s = nullptr;
-  static constexpr int kAux = 4;
-  cudaStream_t aux[kAux] = {};
-  cudaEvent_t fork = nullptr, join[kAux] = {};
-  std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
-  ~sf_context() {
-    cache.reset();
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(dev);
-    for (int i = 0; i < kAux; ++i) {
-      if (aux[i]) cudaStreamDestroy(aux[i]);
-      if (join[i]) cudaEventDestroy(join[i]);
-    }
-    if (fork) cudaEventDestroy(fork);
-    if (s) cudaStreamDestroy(s);
-    cudaSetDevice(prev);
-  }
-};
-
-namespace {
+namespace sfe {
 
 int make_context(int device, sf_context** out) {
   int n = 0;
@@ -241,7 +83,7 @@ int choose_myers_class(uint32_t m, int& b, int& lanes) {
   return fail(SF_ERR_TOO_LONG, "pattern too long for the Myers kernels");
 }
 
-DJob make_djob(const Pass& p, const sf_plan& P, uint32_t& flags) {
+DJob make_djob(const Pass& p, uint32_t& flags) {
   DJob j{};
   j.m = p.m;
   j.n = p.n;
@@ -263,7 +105,6 @@ DJob make_djob(const Pass& p, const sf_plan& P, uint32_t& flags) {
     if (p.cut != SF_NOLIMIT) flags |= F_CUT | F_ROWMAX;
     j.cut = p.cut;
   }
-  (void)P;
   return j;
 }
 
@@ -352,7 +193,7 @@ int plan_build(sf_plan* P) {
       continue;
     }
     uint32_t flags = 0;
-    DJob j = make_djob(p, *P, flags);
+    DJob j = make_djob(p, flags);
     j.p_word = word_of[2 * q];
     j.t_word = word_of[2 * q + 1];
     j.p_byte = p.p_off;
@@ -829,7 +670,161 @@ Pass affine_pass(uint64_t p_off, uint64_t m, uint64_t t_off, uint64_t n, int mod
   return p;
 }
 
-}  // namespace
+int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
+                          uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps) {
+  ps.clear();
+  ps.reserve(count);
+  for (uint64_t q = 0; q < count; ++q) {
+    const sf_job_t& j = jobs[q];
+    Pass p;
+    p.p_off = j.p_off;
+    p.t_off = j.t_off;
+    p.m = j.m;
+    p.n = j.n;
+    if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+    if (j.p_off + j.m > pool_bytes || j.t_off + j.n > pool_bytes)
+      return fail(SF_ERR_INVALID, "job sequence outside the pool");
+    if (j.kind != SF_JOB_MYERS) {
+      if (j.sc_index >= n_scores || !ok_sc(&scores[j.sc_index]))
+        return fail(SF_ERR_INVALID, "bad scoring index");
+      p.sc = scores[j.sc_index];
+    }
+    switch (j.kind) {
+      case SF_JOB_MYERS:
+        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
+        p.kind = PK_MYERS;
+        p.mode = j.mode;
+        p.k = j.k;
+        break;
+      case SF_JOB_AFFINE:
+        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
+        p.kind = PK_AFFINE;
+        p.mode = j.mode;
+        p.band = j.band;
+        p.geom = j.n;
+        p.want_cigar = j.want_cigar != 0;
+        p.tb_kind = 0;
+        break;
+      case SF_JOB_EXTEND_WINDOW:
+        p.kind = PK_AFFINE;
+        p.mode = SF_PREFIX;
+        p.band = j.band;
+        p.geom = std::max<uint64_t>(j.window, j.n);
+        p.clip = true;
+        p.cell = true;
+        p.xdrop = j.xdrop;
+        p.end_bonus = j.end_bonus;
+        p.want_cigar = j.want_cigar != 0;
+        p.tb_kind = 1;
+        break;
+      case SF_JOB_LOCAL:
+        p.kind = PK_LOCAL;
+        p.dlo = j.dlo;
+        p.dhi = j.dhi;
+        p.bonus0 = j.end_bonus;
+        p.bonus1 = j.end_bonus2;
+        break;
+      default:
+        return fail(SF_ERR_INVALID, "bad job kind");
+    }
+    ps.push_back(p);
+  }
+  return SF_OK;
+}
+
+int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
+                 uint64_t total) {
+  if (total && (!ops || ops_cap < total)) {
+    return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
+  }
+  if (total) std::memcpy(ops, P->h_ops.p, total * 4);
+  const DRes* rs = P->h_res.as<DRes>();
+  const TRes* tr = P->h_tres.as<TRes>();
+  const uint32_t* mo = P->h_mout.as<uint32_t>();
+  uint64_t acc = 0;
+  // Compacted op order = walk-list order = pass order among CIGAR passes.
+  for (size_t q = 0; q < P->passes.size(); ++q) {
+    const Pass& p = P->passes[q];
+    sf_result_t& o = results[q];
+    std::memset(&o, 0, sizeof o);
+    const uint32_t s = P->slot[q];
+    if (p.kind == PK_MYERS) {
+      o.distance = mo[s];
+      o.score = 0;
+      o.cells = (uint64_t)p.m * p.n;
+      continue;
+    }
+    const DRes& d = rs[s];
+    o.distance = SF_NONE;
+    o.cells = d.cells;
+    o.text_read = d.text_read;
+    if (p.kind == PK_LOCAL) {
+      o.score = d.score;
+    } else if (p.tb_kind == 1) {
+      const int32_t whole = sat_add32(d.score, p.end_bonus);
+      if (d.clip_best >= whole) {
+        o.score = d.clip_best;
+        o.pattern_end = d.clip_i;
+        o.text_end = d.clip_j;
+      } else {
+        o.score = whole;
+        o.pattern_end = p.m;
+        o.text_end = d.score_col;
+      }
+    } else {
+      o.score = d.score;
+      o.pattern_end = p.m;
+      o.text_end = d.score_col;
+    }
+    if (p.want_cigar && p.kind != PK_LOCAL) {
+      const TRes& t = tr[s];
+      o.status = t.status;
+      o.text_start = t.text_start;
+      o.cigar_off = acc;
+      o.n_ops = t.status == 0 ? t.n_ops : 0;
+      acc += o.n_ops;
+    }
+  }
+  return SF_OK;
+}
+
+uint64_t plan_bytes_held(const sf_plan* P) {
+  const DevBuf* bufs[] = {&P->d_bytes, &P->d_pool, &P->d_seq, &P->d_djobs, &P->d_params,
+                          &P->d_res, &P->d_mjobs, &P->d_mout, &P->d_tjobs, &P->d_tres,
+                          &P->d_tb, &P->d_ops, &P->d_opsc, &P->d_offs, &P->d_order,
+                          &P->d_counters, &P->d_wlist, &P->d_cls, &P->d_scratch, &P->d_total};
+  uint64_t b = 0;
+  for (const DevBuf* d : bufs) b += d->cap;
+  return b;
+}
+
+uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_bytes) {
+  // Mirrors plan_build's sizes: byte pool, packed pool, descriptors, results, traceback
+  // arena, CIGAR slots (twice: slots and compacted), wide-row scratch; DevBuf keeps 25%
+  // headroom on each.
+  uint64_t b = pool_bytes + 256 * 4 + 4096;
+  uint64_t scratch = 0;
+  for (const Pass& p : passes) {
+    b += (uint64_t)(p.m + p.n + 34) / 4 + 40 + 200;
+    if (p.kind == PK_MYERS) continue;
+    uint32_t flags = 0;
+    DJob j = make_djob(p, flags);
+    const int64_t wmax = band_wmax(j, flags);
+    int c = 4;
+    bool wide = false;
+    choose_affine_class(wmax, c, wide);
+    if (p.want_cigar && p.kind != PK_LOCAL) {
+      b += (uint64_t)p.m * tb_row_words(c, wide ? wide_chunks(c, wmax) : 1) * 4;
+      b += 2 * ((uint64_t)p.m + p.n + 2) * 4;
+    }
+    if (wide) scratch = std::max<uint64_t>(scratch, (uint64_t)wide_chunks(c, wmax) * 32 * c);
+  }
+  // Wide buckets (with and without traceback): up to 2 blocks/SM x 4 warps x 4 rows each.
+  b += scratch * 4 * 2 * 304 * 4 * 4 * 2;
+  return b + b / 4;
+}
+
+}  // namespace sfe
 
 int sf_internal_set_error(int code, const char* msg) { return fail(code, msg); }
 
@@ -1159,68 +1154,6 @@ int sf_affine_extend_window_cigar(const uint8_t* pattern, uint64_t m, const uint
 
 // ---- plans ------------------------------------------------------------------------------
 
-static int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
-                          uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps) {
-  ps.clear();
-  ps.reserve(count);
-  for (uint64_t q = 0; q < count; ++q) {
-    const sf_job_t& j = jobs[q];
-    Pass p;
-    p.p_off = j.p_off;
-    p.t_off = j.t_off;
-    p.m = j.m;
-    p.n = j.n;
-    if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
-    if (j.p_off + j.m > pool_bytes || j.t_off + j.n > pool_bytes)
-      return fail(SF_ERR_INVALID, "job sequence outside the pool");
-    if (j.kind != SF_JOB_MYERS) {
-      if (j.sc_index >= n_scores || !ok_sc(&scores[j.sc_index]))
-        return fail(SF_ERR_INVALID, "bad scoring index");
-      p.sc = scores[j.sc_index];
-    }
-    switch (j.kind) {
-      case SF_JOB_MYERS:
-        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
-        p.kind = PK_MYERS;
-        p.mode = j.mode;
-        p.k = j.k;
-        break;
-      case SF_JOB_AFFINE:
-        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
-        p.kind = PK_AFFINE;
-        p.mode = j.mode;
-        p.band = j.band;
-        p.geom = j.n;
-        p.want_cigar = j.want_cigar != 0;
-        p.tb_kind = 0;
-        break;
-      case SF_JOB_EXTEND_WINDOW:
-        p.kind = PK_AFFINE;
-        p.mode = SF_PREFIX;
-        p.band = j.band;
-        p.geom = std::max<uint64_t>(j.window, j.n);
-        p.clip = true;
-        p.cell = true;
-        p.xdrop = j.xdrop;
-        p.end_bonus = j.end_bonus;
-        p.want_cigar = j.want_cigar != 0;
-        p.tb_kind = 1;
-        break;
-      case SF_JOB_LOCAL:
-        p.kind = PK_LOCAL;
-        p.dlo = j.dlo;
-        p.dhi = j.dhi;
-        p.bonus0 = j.end_bonus;
-        p.bonus1 = j.end_bonus2;
-        break;
-      default:
-        return fail(SF_ERR_INVALID, "bad job kind");
-    }
-    ps.push_back(p);
-  }
-  return SF_OK;
-}
-
 int sf_plan_create(sf_context* ctx, const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
                    uint32_t n_scores, uint64_t pool_bytes, sf_plan** out) {
   if (!ctx || !out || (count && !jobs)) return fail(SF_ERR_INVALID, "bad argument");
@@ -1268,59 +1201,7 @@ int sf_plan_download(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t o
   uint64_t total = 0;
   if ((rc = plan_fetch_ops(P, total))) return rc;
   if (ops_used) *ops_used = total;
-  if (total && (!ops || ops_cap < total)) {
-    if (ops_used) *ops_used = total;
-    return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
-  }
-  if (total) std::memcpy(ops, P->h_ops.p, total * 4);
-  const DRes* rs = P->h_res.as<DRes>();
-  const TRes* tr = P->h_tres.as<TRes>();
-  const uint32_t* mo = P->h_mout.as<uint32_t>();
-  uint64_t acc = 0;
-  // Compacted op order = walk-list order = pass order among CIGAR passes.
-  for (size_t q = 0; q < P->passes.size(); ++q) {
-    const Pass& p = P->passes[q];
-    sf_result_t& o = results[q];
-    std::memset(&o, 0, sizeof o);
-    const uint32_t s = P->slot[q];
-    if (p.kind == PK_MYERS) {
-      o.distance = mo[s];
-      o.score = 0;
-      o.cells = (uint64_t)p.m * p.n;
-      continue;
-    }
-    const DRes& d = rs[s];
-    o.distance = SF_NONE;
-    o.cells = d.cells;
-    o.text_read = d.text_read;
-    if (p.kind == PK_LOCAL) {
-      o.score = d.score;
-    } else if (p.tb_kind == 1) {
-      const int32_t whole = sat_add32(d.score, p.end_bonus);
-      if (d.clip_best >= whole) {
-        o.score = d.clip_best;
-        o.pattern_end = d.clip_i;
-        o.text_end = d.clip_j;
-      } else {
-        o.score = whole;
-        o.pattern_end = p.m;
-        o.text_end = d.score_col;
-      }
-    } else {
-      o.score = d.score;
-      o.pattern_end = p.m;
-      o.text_end = d.score_col;
-    }
-    if (p.want_cigar && p.kind != PK_LOCAL) {
-      const TRes& t = tr[s];
-      o.status = t.status;
-      o.text_start = t.text_start;
-      o.cigar_off = acc;
-      o.n_ops = t.status == 0 ? t.n_ops : 0;
-      acc += o.n_ops;
-    }
-  }
-  return SF_OK;
+  return plan_results(P, results, ops, ops_cap, total);
 }
 
 int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, const sf_job_t* jobs,

@@ -164,3 +164,105 @@ def config3(pairs: int = 100_000, seed: int = 3) -> tuple[Pairs, Pairs]:
         fts.append(np.concatenate([fl[:50], t, fl[50:]]))
     return (_assemble(qs, fts, np.zeros(pairs), "c3-myers"),
             _assemble(qs, ts, c3_band(L.astype(np.float64)), "c3-affine"))
+
+
+# ---- serving stream (config 5) ------------------------------------------------------------
+
+ONT_CDNA = Profile(0.40, 0.25, 0.35, 4.0)  # sim.rs:28-35 `ont`
+
+
+@dataclass
+class Read:
+    read: np.ndarray     # the read, in the transcript's orientation
+    region: np.ndarray   # the transcript bases it came from
+    flanked: np.ndarray  # region with 50 random bases on each side
+
+
+def serving_read(rng: np.random.Generator, hifi: bool) -> Read:
+    """One read of the serving model.  ONT cDNA-like reads (7% error, sim.rs `ont` profile)
+    cover the 3' end of a transcript of 300..12,000 bases (log-normal, median 1,500): the
+    reference simulator keeps the 3' end and truncates the 5' end
+    (crates/spearfish-cli/src/simulate_cmd.rs:4-6).  HiFi-like reads are 1..20 kb at 1%
+    error."""
+    if hifi:
+        L = int(rng.integers(1000, 20001))
+        region = rng.integers(0, 4, L, dtype=np.uint8)
+        read = simulate(region, 0.01, HIFI, rng)
+    else:
+        T = int(np.clip(np.exp(np.log(1500.0) + 0.6 * rng.standard_normal()), 300, 12000))
+        keep = int(T * rng.uniform(0.5, 1.0))
+        region = rng.integers(0, 4, keep, dtype=np.uint8)
+        read = simulate(region, 0.07, ONT_CDNA, rng)
+    fl = rng.integers(0, 4, 100, dtype=np.uint8)
+    return Read(read, region, np.concatenate([fl[:50], region, fl[50:]]))
+
+
+def serving_jobs(reads: list, B) -> tuple[np.ndarray, np.ndarray]:
+    """The jobs a read batch hands the alignment stage, per read: a Myers Infix distance of the
+    read against its flanked region (map/src/lib.rs:913-935 `whole_read`), a banded Global
+    affine pass with CIGAR over the region (band as in the uneven batch), and X-drop
+    extensions of its two 100-base ends into windows of x + 20 + x/10 bases
+    (map/src/lib.rs:2100-2114 `extend_dp`, TieBreak/Ends defaults: band 16, X-drop 50,
+    end bonus 5), with CIGARs."""
+    pool = []
+    at = 0
+    rows = []
+
+    def put(a):
+        nonlocal at
+        pool.append(a)
+        off = at
+        at += a.size
+        return off
+
+    for r in reads:
+        m = r.read.size
+        po = put(r.read)
+        rows.append((po, m, put(r.flanked), r.flanked.size, B.JOB_MYERS, 0, 0, 0, 0, 0, 0))
+        band = int(c3_band(np.array([float(m)]))[0])
+        rows.append((po, m, put(r.region), r.region.size, B.JOB_AFFINE, 2, 1, band, 0, 0, 0))
+        x = min(100, m)
+        w = x + 20 + x // 10
+        # right end: the read's last x bases against the region's last w bases
+        tail = r.region[max(0, r.region.size - w):]
+        rows.append((po + m - x, x, put(tail), tail.size, B.JOB_EXTEND_WINDOW, 1, 1, 16, w,
+                     5, 50))
+        # left end: reversed, as the mapper extends leftwards (map/src/lib.rs:3266-3274)
+        head_r = np.ascontiguousarray(r.read[:x][::-1])
+        head_t = np.ascontiguousarray(r.region[:w][::-1])
+        rows.append((put(head_r), x, put(head_t), head_t.size, B.JOB_EXTEND_WINDOW, 1, 1, 16,
+                     w, 5, 50))
+    jobs = B.new_jobs(len(rows))
+    for q, (po, m, to, n, kind, mode, cig, band, win, bonus, xd) in enumerate(rows):
+        j = jobs[q]
+        j["p_off"], j["m"], j["t_off"], j["n"] = po, m, to, n
+        j["kind"], j["mode"], j["want_cigar"] = kind, mode, cig
+        if kind != B.JOB_MYERS:
+            j["band"] = band
+        if kind == B.JOB_EXTEND_WINDOW:
+            j["window"], j["end_bonus"], j["xdrop"] = win, bonus, xd
+    return (np.concatenate(pool) if pool else np.zeros(1, np.uint8)), jobs
+
+
+def serving_stream(duration_s: float, reads_per_s: float = 2000.0, burst: float = 5.0,
+                   max_batch: int = 4096, seed: int = 5):
+    """Arrivals of read batches: batch sizes log-uniform over 1..max_batch reads, batch
+    arrivals Poisson, the rate switching between a base rate and `burst` times it (bursts of
+    exponential length, mean 0.5 s, 10% of the time) so that the mean is `reads_per_s`.
+    Returns [(arrival seconds, reads in the batch)]."""
+    rng = np.random.default_rng(seed)
+    mean_batch = (max_batch - 1) / np.log(max_batch)
+    base = reads_per_s / mean_batch / (0.9 + 0.1 * burst)
+    t, out, bursting, switch = 0.0, [], False, rng.exponential(4.5)
+    while t < duration_s:
+        rate = base * (burst if bursting else 1.0)
+        dt = rng.exponential(1.0 / rate)
+        if t + dt > switch:
+            t = switch
+            bursting = not bursting
+            switch = t + rng.exponential(0.5 if bursting else 4.5)
+            continue
+        t += dt
+        size = int(np.clip(np.round(np.exp(rng.uniform(0, np.log(max_batch)))), 1, max_batch))
+        out.append((t, size))
+    return out
