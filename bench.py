@@ -438,11 +438,20 @@ def main():
     except OSError:
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tr = json.load(f).get(stages[top])
+        if tr:
+            traffic = int(tr["bytes_per_cell"] * top_cells)
+    except (OSError, ValueError):
+        pass
     roofline = {"bound": "int32", "kernel": stages[top], "achieved": achieved,
                 "peak": peak.value, "unit": "Tops/s", "frac": achieved / peak.value if peak.value else None,
                 "peak_source": "measured on this GPU by sf_int_peak (int32 add-then-max mix)",
                 "ops_per_cell": ops_cell, "cells_per_launch": top_cells,
-                "kernel_ms": avg[top], "traffic": None,
+                "kernel_ms": avg[top], "traffic": traffic,
+                "traffic_source": "profiles/traffic.json (ncu small case, scaled by cells)",
                 "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak,
                         "frac": (hbm_gbs / hbm_peak) if hbm_gbs else None,
                         "note": "traceback nibbles written + packed inputs read"},
