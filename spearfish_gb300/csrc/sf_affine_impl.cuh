@@ -1031,7 +1031,7 @@ __device__ void pair_wide(const sfk::AffLaunch& a, uint32_t jid, int lane, int32
 template <int C, bool WIDE>
 struct MinBlocks {
   static constexpr int value =
-      WIDE ? 3 : (C <= 12 ? 6 : (C <= 16 ? 5 : (C <= 20 ? 4 : (C <= 32 ? 3 : 2))));
+      WIDE ? 3 : (C <= 12 ? 6 : (C <= 16 ? 5 : (C <= 20 ? 4 : 3)));
 };
 
 template <int C, bool WIDE, bool TB, bool LOCAL>

@@ -10,6 +10,8 @@
 // exact whenever the distance is <= k and reports None otherwise (align.rs:87-168, pinned by
 // its tests `random_vs_naive` / `related_vs_naive`), so comparing the full-column distance
 // with k gives the same Option<u32>.
+#include <type_traits>
+
 #include "sf_internal.cuh"
 
 namespace {
@@ -114,45 +116,52 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     int steps = has && m > 0 ? (int)n + P - 1 : 0;
     steps = __reduce_max_sync(FULL, steps);
     uint32_t payload = 0;  // (text code << 2) | (h + 1)
-    for (int t = 0; t < steps; ++t) {
+    uint32_t tw = 0;       // the text word holding base t + 1 (used by lane 0)
+    const bool glob = J.mode == 2;
+    // One step of the pipeline.  Lanes keep their state only while they are past the fill
+    // (FILL: some lanes have not reached column 0 yet); past its text's end a lane computes
+    // on state nothing reads any more, so the steady loop needs no masking and no branches.
+    auto step = [&](int t, auto fill) {
+      constexpr bool FILL = decltype(fill)::value;
       const int j = t - l;
-      const bool active = has && m > 0 && j >= 0 && j < (int)n;
+      const bool live = has && m > 0 && j >= 0 && j < (int)n;
       const uint32_t in = __shfl_up_sync(FULL, payload, 1, P);
-      uint32_t c;
-      int h;
-      if (l == 0) {
-        c = active ? sf::base_at(a.pool, J.t_word, (uint64_t)j + 1) : 0;
-        h = top;
-      } else {
-        c = in >> 2;
-        h = (int)(in & 3) - 1;
-      }
-      if (active) {
-        int hlast = 0;
+      // A new text word every 16 steps, read only while it lies inside this text (base t + 1
+      // of a text of n bases sits in word (t + 1) / 16 after the leading pad base).
+      if ((((t + 1) & 15) == 0 || t == 0) && (uint32_t)(t + 1) <= n)
+        tw = __ldg(a.pool + J.t_word + ((uint32_t)(t + 1) >> 4));
+      const uint32_t c0 = (tw >> (2 * ((t + 1) & 15))) & 3u;
+      const uint32_t c = l == 0 ? c0 : (in >> 2);
+      int h = l == 0 ? top : (int)(in & 3) - 1;
+      int hlast = 0;
 #pragma unroll
-        for (int bb = 0; bb < B; ++bb) {
-          const uint32_t b = (uint32_t)l * B + bb;
-          if (b < blocks) {
-            uint64_t eq;
-            if constexpr (SMEM)
-              eq = speq[((size_t)bb * 4 + c) * 32 + lane];
-            else
-              eq = c == 0 ? peq[bb][0] : c == 1 ? peq[bb][1] : c == 2 ? peq[bb][2] : peq[bb][3];
-            h = myers_step(pv[bb], mv[bb], eq, h, outbit[bb]);
-            if (bb == own_bb) hlast = h;
+      for (int bb = 0; bb < B; ++bb) {
+        uint64_t eq;
+        if constexpr (SMEM)
+          eq = speq[((size_t)bb * 4 + c) * 32 + lane];
+        else
+          eq = c == 0 ? peq[bb][0] : c == 1 ? peq[bb][1] : c == 2 ? peq[bb][2] : peq[bb][3];
+        if constexpr (FILL) {
+          uint64_t p2 = pv[bb], m2 = mv[bb];
+          h = myers_step(p2, m2, eq, h, outbit[bb]);
+          if (j >= 0) {
+            pv[bb] = p2;
+            mv[bb] = m2;
           }
+        } else {
+          h = myers_step(pv[bb], mv[bb], eq, h, outbit[bb]);
         }
-        if (owner) {
-          score += hlast;
-          if (J.mode == 2) {
-            if (j + 1 == (int)n) best = score;
-          } else {
-            best = min(best, score);
-          }
-        }
+        hlast = bb == own_bb ? h : hlast;
       }
+      const bool upd = owner && live;
+      score = upd ? score + hlast : score;
+      best = upd ? (glob ? (j + 1 == (int)n ? score : best) : min(best, score)) : best;
       payload = (c << 2) | (uint32_t)(h + 1);
-    }
+    };
+    const int fill = steps < P - 1 ? steps : P - 1;
+    int t = 0;
+    for (; t < fill; ++t) step(t, std::true_type{});
+    for (; t < steps; ++t) step(t, std::false_type{});
     if (has) {
       if (m == 0) {
         if (l == 0) {
