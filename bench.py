@@ -151,11 +151,25 @@ def workload(cfg: str, scale: float, cigar: bool = True):
     return pool, np.concatenate([jm, ja]), [my, af], "mixed"
 
 
-AFFINE_C = (4, 6, 8, 9, 10, 11, 12, 14, 16, 20, 24, 28, 32, 40, 48)  # register-row classes of libsf_align (sf_walk.cu)
+AFFINE_C = (4, 6, 8, 9, 10, 11, 12, 14, 16, 20, 24, 28, 32, 40, 48)  # 32-bit register classes
+AFFINE16_C = (4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48, 56, 64)  # packed 16-bit classes
+
+
+def fits16(j, w, sc, B) -> bool:
+    """sf_host.cu fits16: Global/Prefix banded passes whose values fit 16-bit fields."""
+    if j["kind"] == B.JOB_LOCAL or j["mode"] == 0 or int(j["band"]) == 2 ** 64 - 1:
+        return False
+    mat, mis, opn, ext = sc
+    if min(sc) < 0 or max(sc) > 1000 or w > 32 * AFFINE16_C[-1]:
+        return False
+    go = opn + ext
+    step = max(mat, mis, go)
+    return (mat + ext) * w + go + 2 * 64 * step + 2 * (go + mis + ext) + mat + 256 <= 16384 \
+        and os.environ.get("SF_AFFINE16", "1")[:1] != "0"
 MYERS_B = (1, 2, 3, 4, 6, 8, 12, 16)
 
 
-def job_classes(jobs, B):
+def job_classes(jobs, B, scores=((2, 4, 4, 2),)):
     """The kernel class each job runs in, by the library's bucketing rule (sf_host.cu)."""
     out = []
     for j in jobs:
@@ -180,6 +194,9 @@ def job_classes(jobs, B):
             w = 2 * band + 1 + abs(m - geom)
         w = max(0, min(w, n + 1))
         tbf = bool(j["want_cigar"]) and j["kind"] != B.JOB_LOCAL
+        if fits16(j, w, scores[int(j["sc_index"])], B):
+            out.append(("affine16", next(c for c in AFFINE16_C if 32 * c >= w), False, tbf))
+            continue
         c = next((c for c in AFFINE_C if 32 * c >= w), None)
         out.append(("affine", c, False, tbf) if c else ("affine", 16, True, tbf))
     return out
@@ -414,14 +431,16 @@ def main():
     desc = json.loads(plan.describe())
     stages = ["pack"] + [f"{b['kind']}-c{b['c']}{'-wide' if b['wide'] else ''}"
                          f"{'-tb' if b['traceback'] else ''}" for b in desc["buckets"]]
-    if len(prof[0]) > len(stages):
+    if len(prof[0]) == len(stages) + 2:
+        stages += ["walk", "cigar-compact"]
+    elif len(prof[0]) > len(stages):
         stages.append("cigar-compact")
     avg = [statistics.mean(p[i] for p in prof) for i in range(len(prof[0]))]
     top = max(range(1, 1 + len(desc["buckets"])), key=lambda i: avg[i])
     tb = desc["buckets"][top - 1]
     cls = job_classes(jobs, B)
     key = ("myers", tb["c"], tb["lanes"]) if tb["kind"] == "myers" else \
-        ("affine", tb["c"], bool(tb["wide"]), bool(tb["traceback"]))
+        (tb["kind"], tb["c"], bool(tb["wide"]), bool(tb["traceback"]))
     sel = np.array([c == key for c in cls])
     top_cells = int(out.results["cells"][sel].astype(np.uint64).sum())
     ops_cell = OPS_PER_CELL["myers"] if tb["kind"] == "myers" else (
@@ -429,8 +448,14 @@ def main():
     achieved = top_cells * ops_cell / (avg[top] * 1e-3) / 1e12
     peak = C.c_double()
     lib.sf_int_peak(local, C.byref(peak), None)
-    tb_bytes = desc.get("traceback_bytes", 0)
-    hbm_gbs = (tb_bytes + pool.size / 4) / (avg[top] * 1e-3) / 1e9 if tb["traceback"] else None
+    # HBM side of the same kernel: algorithmic bytes = its pairs' packed inputs (2 bits a base)
+    # + 8 B of result each + half a byte of traceback bits per DP cell when it keeps them;
+    # measured bytes = the ncu DRAM bytes per cell of this kernel, scaled to this launch.
+    sel_jobs = jobs[sel]
+    alg_bytes = int((sel_jobs["m"].astype(np.uint64) + sel_jobs["n"]).sum()) // 4 + 8 * len(sel_jobs)
+    if tb.get("traceback"):
+        alg_bytes += top_cells // 2
+    hbm_gbs = alg_bytes / (avg[top] * 1e-3) / 1e9
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -452,9 +477,13 @@ def main():
                 "ops_per_cell": ops_cell, "cells_per_launch": top_cells,
                 "kernel_ms": avg[top], "traffic": traffic,
                 "traffic_source": "profiles/traffic.json (ncu small case, scaled by cells)",
-                "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak,
-                        "frac": (hbm_gbs / hbm_peak) if hbm_gbs else None,
-                        "note": "traceback nibbles written + packed inputs read"},
+                "hbm": {"algorithmic_bytes": alg_bytes, "achieved_gbs": hbm_gbs,
+                        "measured_gbs": (traffic / (avg[top] * 1e-3) / 1e9) if traffic else None,
+                        "peak_gbs": hbm_peak, "frac": hbm_gbs / hbm_peak,
+                        "measured_frac": (traffic / (avg[top] * 1e-3) / 1e9 / hbm_peak)
+                        if traffic else None,
+                        "note": "top kernel only: packed inputs + results + 0.5 B/cell of "
+                                "traceback bits (algorithmic); measured = ncu DRAM bytes"},
                 "stages_ms": dict(zip(stages, [round(a, 4) for a in avg]))}
 
     # e2e through the C ABI from pinned host buffers.

@@ -261,8 +261,9 @@ uint64_t sf_plan_launches(const sf_plan *plan);
 const char *sf_plan_describe(sf_plan *plan);
 
 /* Runs one execute in order on the plan's stream with CUDA events between
- * its stages -- pack, each bucket (in sf_plan_describe's order), then the
- * traceback walk with CIGAR compaction -- and returns each stage's ms. */
+ * its stages -- pack, each bucket (in sf_plan_describe's order; a bucket
+ * that keeps CIGARs walks its paths too), then the CIGAR compaction -- and
+ * returns each stage's ms. */
 int sf_plan_profile(sf_plan *plan, float *ms, uint32_t cap,
                     uint32_t *n_stages);
 

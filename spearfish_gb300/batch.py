@@ -109,7 +109,7 @@ class Plan:
 
     def profile(self) -> list[float]:
         """One execute in order with events between stages: ms of pack, each bucket (in
-        `describe()` order), then walk + CIGAR compaction."""
+        `describe()` order, walks included), then the CIGAR compaction."""
         ms = (C.c_float * 256)()
         n = C.c_uint32()
         _abi.check(self._lib.sf_plan_profile(self.handle, ms, 256, C.byref(n)))

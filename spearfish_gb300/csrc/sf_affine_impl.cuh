@@ -19,12 +19,13 @@
 //
 // Traceback: four decisions per cell -- "F extended" (vs opened from H above), "diagonal
 // lost" (H' came from F), "E extended" (vs opened from H' on the left), "H came from E" --
-// kept as sign bits in bit-plane words (tb_push), stored per row as 32 lanes x 2 words per
-// 16 cells, lane-fastest, and walked into a CIGAR by the same warp (walk_warp).
+// kept as sign bits in bit-plane words (tb_push), stored per row as one (A, B) word pair per
+// lane and 16 cells, lane-fastest; the same warp then walks them into a CIGAR (sf_walk.cuh).
 #pragma once
 #include <type_traits>
 
 #include "sf_internal.cuh"
+#include "sf_walk.cuh"
 
 namespace {
 
@@ -336,327 +337,6 @@ __device__ __forceinline__ int32_t clamp30(int64_t v) {
   return (int32_t)(v < -k ? -k : (v > k ? k : v));
 }
 
-// ---------------------------------------------------------------------------------------
-// Traceback walk (no reference counterpart: spearfish computes no alignment path).  The warp
-// that computed a pass walks it right after, on lane 0: from the end cell back to row 0 /
-// column 0 through the pass's nibbles, with the tie order they encode (H from H' before E,
-// diagonal before vertical, opening before extending), writing the CIGAR run-length encoded,
-// BAM-style (len << 4 | op).  The walk is memory-latency bound while the passes are ALU
-// bound, so the other warps' rows hide it.  Every nibble address is range-checked against
-// the row's band before it is read; a path that leaves the band reports "no path".
-// A cell's decisions from its group's two bit-plane words, as a nibble: bit 0 "H' came from F",
-// bit 1 "H came from E", bit 2 "E opened", bit 3 "F opened".
-template <int C>
-__device__ __forceinline__ uint32_t tb_decode(uint32_t wa, uint32_t wb, int c) {
-  const int g = c >> 4, p = c & 15;
-  const int gs = (C - 16 * g) < 16 ? (C - 16 * g) : 16;
-  const int sh = 2 * (gs - 1 - p);
-  const uint32_t a = (wa >> sh) & 3u, b = (wb >> sh) & 3u;  // (first << 1) | second
-  // a: (F extended, diagonal lost); b: (E extended, H from E)
-  return (a & 1u) | ((b & 1u) << 1) | (((b >> 1) ^ 1u) << 2) | (((a >> 1) ^ 1u) << 3);
-}
-
-struct OpWriter {
-  uint32_t* out;
-  uint32_t cap, n = 0;
-  int status = 0;
-  __device__ void push(uint32_t op, uint32_t len) {
-    if (len == 0 || status) return;
-    if (n > 0 && (out[n - 1] & 15u) == op) {
-      out[n - 1] += len << 4;
-      return;
-    }
-    if (n == cap) {
-      status = -1;
-      return;
-    }
-    out[n++] = (len << 4) | op;
-  }
-};
-
-template <int C, bool WIDE>
-__device__ void walk_pass(const sfk::AffLaunch& a, uint32_t jid, const PassCtx& x, const Geo32& g,
-                          const DRes& R) {
-  constexpr int CW = 2 * ((C + 15) / 16);
-  const TJob T = a.tjobs[jid];
-  const int32_t m = (int32_t)x.m;
-  const uint64_t stride_w =
-      WIDE ? tb_row_words(C, wide_chunks(C, band_wmax(x.J, x.P.flags))) : tb_row_words(C, 1);
-  // End cell (align.rs:2643-2650 score_col; 975-981 the window's choice).
-  int32_t score, ei, ej, tail = 0;
-  bool ok = true;
-  if (T.kind == 0) {
-    score = R.score;
-    ei = m;
-    ej = (int32_t)R.score_col;
-    ok = R.score > NEG / 2;
-  } else {
-    const int32_t whole = sat_add(R.score, T.end_bonus);
-    if (R.clip_best >= whole) {
-      score = R.clip_best;
-      ei = (int32_t)R.clip_i;
-      ej = (int32_t)R.clip_j;
-      tail = m - ei;
-    } else {
-      score = whole;
-      ei = m;
-      ej = (int32_t)R.score_col;
-      ok = R.score > NEG / 2;
-    }
-  }
-  OpWriter w{a.ops + T.ops_off, T.ops_cap};
-  int32_t text_start = 0;
-  if (!ok) {
-    w.status = 1;
-  } else {
-    w.push(4, (uint32_t)tail);
-    int32_t i = ei, j = ej;
-    int state = 0;  // 0 H, 1 E, 2 F
-    const int64_t guard = 2 * ((int64_t)m + x.J.n) + 8;
-    for (int64_t it = 0;; ++it) {
-      if (it > guard) {
-        w.status = 1;
-        break;
-      }
-      if (state == 0 && i == 0) {
-        if (x.mode == 0)
-          text_start = j;
-        else
-          w.push(2, (uint32_t)j);
-        break;
-      }
-      if (state == 0 && j == 0) {
-        w.push(1, (uint32_t)i);
-        break;
-      }
-      if (i <= 0 || j <= 0) {
-        w.status = 1;
-        break;
-      }
-      int32_t lo, hi;
-      g.range(i, lo, hi);
-      const int32_t K = j - lo;
-      if (K < 0 || j > hi) {
-        w.status = 1;
-        break;
-      }
-      uint64_t word;
-      int c;
-      constexpr int TG = (C + 15) / 16;
-      if constexpr (WIDE) {
-        const int32_t qc = K / (32 * C), r = K % (32 * C);
-        c = r % C;
-        word = x.J.tb_word + (uint64_t)(i - 1) * stride_w + (uint64_t)qc * CW * 32 +
-               (uint64_t)(c >> 4) * 32 + (uint64_t)(r / C);
-      } else {
-        c = K % C;
-        word = x.J.tb_word + (uint64_t)(i - 1) * stride_w + (uint64_t)(c >> 4) * 32 +
-               (uint64_t)(K / C);
-      }
-      const uint32_t nib = tb_decode<C>(a.tb[word], a.tb[word + TG * 32], c);
-      if (state == 0) {
-        if (nib & 2u) {
-          state = 1;
-        } else if (!(nib & 1u)) {
-          w.push(0, 1);
-          --i;
-          --j;
-        } else {
-          state = 2;
-        }
-      } else if (state == 1) {
-        w.push(2, 1);
-        state = (nib & 4u) ? 0 : 1;
-        --j;
-      } else {
-        w.push(1, 1);
-        state = (nib & 8u) ? 0 : 2;
-        --i;
-      }
-      if (w.status) break;
-    }
-  }
-  if (w.status == 0) {
-    for (uint32_t p = 0, q = w.n ? w.n - 1 : 0; p < q; ++p, --q) {
-      const uint32_t t = w.out[p];
-      w.out[p] = w.out[q];
-      w.out[q] = t;
-    }
-  }
-  TRes tr;
-  tr.score = score;
-  tr.status = w.status;
-  tr.end_i = (uint32_t)ei;
-  tr.end_j = (uint32_t)ej;
-  tr.text_start = (uint32_t)text_start;
-  tr.n_ops = w.status == 0 ? w.n : 0;
-  a.tres[jid] = tr;
-}
-
-// The same walk by a whole warp, for register rows.  The warp keeps a cache of 32 rows x 3
-// lanes' traceback words: lane q holds row rbase - q, for the band lanes L0 - 1 .. L0 + 1 around
-// the path.  A path moves up one row per diagonal or vertical step and drifts sideways slowly,
-// so one round of 32 parallel loads serves ~32 rows; each step then costs a shuffle, not a
-// dependent memory round trip.  All lanes run the walk in lockstep (the state is uniform);
-// lane 0 writes the CIGAR, run-length merged in registers.
-template <int C>
-__device__ void walk_warp(const sfk::AffLaunch& a, uint32_t jid, const PassCtx& x, const Geo32& g,
-                          const DRes& R, int lane) {
-  constexpr int CW = 2 * ((C + 15) / 16);
-  constexpr int NC = 3 * CW;
-  const TJob T = a.tjobs[jid];
-  const int32_t m = (int32_t)x.m;
-  const uint32_t* tb = a.tb + x.J.tb_word;
-  int32_t score, ei, ej, tail = 0;
-  bool ok = true;
-  if (T.kind == 0) {
-    score = R.score;
-    ei = m;
-    ej = (int32_t)R.score_col;
-    ok = R.score > NEG / 2;
-  } else {
-    const int32_t whole = sat_add(R.score, T.end_bonus);
-    if (R.clip_best >= whole) {
-      score = R.clip_best;
-      ei = (int32_t)R.clip_i;
-      ej = (int32_t)R.clip_j;
-      tail = m - ei;
-    } else {
-      score = whole;
-      ei = m;
-      ej = (int32_t)R.score_col;
-      ok = R.score > NEG / 2;
-    }
-  }
-  uint32_t* out = a.ops + T.ops_off;
-  const uint32_t cap = T.ops_cap;
-  uint32_t n_ops = 0, cur_op = 15, cur_len = 0;
-  int status = ok ? 0 : 1;
-  auto flush = [&]() {
-    if (cur_len == 0) return;
-    if (n_ops == cap) {
-      status = -1;
-      return;
-    }
-    if (lane == 0) out[n_ops] = (cur_len << 4) | cur_op;
-    ++n_ops;
-  };
-  auto push = [&](uint32_t op, uint32_t len) {
-    if (len == 0 || status) return;
-    if (op == cur_op) {
-      cur_len += len;
-      return;
-    }
-    flush();
-    cur_op = op;
-    cur_len = len;
-  };
-  int32_t text_start = 0;
-  if (ok) {
-    push(4, (uint32_t)tail);
-    int32_t i = ei, j = ej;
-    int state = 0;  // 0 H, 1 E, 2 F
-    int32_t rbase = -1, L0 = -100;
-    uint32_t cache[NC];
-    const int64_t guard = 2 * ((int64_t)m + x.J.n) + 8;
-    for (int64_t it = 0; !status; ++it) {
-      if (it > guard) {
-        status = 1;
-        break;
-      }
-      if (state == 0 && i == 0) {
-        if (x.mode == 0)
-          text_start = j;
-        else
-          push(2, (uint32_t)j);
-        break;
-      }
-      if (state == 0 && j == 0) {
-        push(1, (uint32_t)i);
-        break;
-      }
-      if (i <= 0 || j <= 0) {
-        status = 1;
-        break;
-      }
-      int32_t lo, hi;
-      g.range(i, lo, hi);
-      const int32_t K = j - lo;
-      if (K < 0 || j > hi) {
-        status = 1;
-        break;
-      }
-      const int32_t Lk = K / C, c = K % C;
-      if (i > rbase || i < rbase - 31 || Lk < L0 - 1 || Lk > L0 + 1) {
-        // Refill: lane q loads row i - q's words for band lanes Lk - 1 .. Lk + 1.
-        rbase = i;
-        L0 = Lk;
-        const int32_t r = i - lane;
-#pragma unroll
-        for (int dl = 0; dl < 3; ++dl) {
-          const int32_t L = L0 - 1 + dl;
-#pragma unroll
-          for (int w = 0; w < CW; ++w)
-            cache[dl * CW + w] = (r >= 1 && L >= 0 && L < 32)
-                                     ? tb[(uint64_t)(r - 1) * (CW * 32) + w * 32 + L]
-                                     : 0u;
-        }
-      }
-      constexpr int TG = (C + 15) / 16;
-      const int idx = (Lk - L0 + 1) * CW + (c >> 4);
-      uint32_t va = cache[0], vb = cache[TG];
-#pragma unroll
-      for (int q = 1; q < NC; ++q) {
-        if (q == idx) va = cache[q];
-        if (q == idx + TG) vb = cache[q];
-      }
-      const uint32_t wa = __shfl_sync(FULL, va, rbase - i);
-      const uint32_t wb = __shfl_sync(FULL, vb, rbase - i);
-      const uint32_t nib = tb_decode<C>(wa, wb, c);
-      if (state == 0) {
-        if (nib & 2u) {
-          state = 1;
-        } else if (!(nib & 1u)) {
-          push(0, 1);
-          --i;
-          --j;
-        } else {
-          state = 2;
-        }
-      } else if (state == 1) {
-        push(2, 1);
-        state = (nib & 4u) ? 0 : 1;
-        --j;
-      } else {
-        push(1, 1);
-        state = (nib & 8u) ? 0 : 2;
-        --i;
-      }
-    }
-    if (!status) flush();
-  }
-  __syncwarp();
-  if (status == 0) {
-    // Reverse in place, the lanes swapping pairs in parallel.
-    for (uint32_t p = lane; p < n_ops / 2; p += 32) {
-      const uint32_t q = n_ops - 1 - p;
-      const uint32_t t = out[p];
-      out[p] = out[q];
-      out[q] = t;
-    }
-  }
-  if (lane == 0) {
-    TRes tr;
-    tr.score = score;
-    tr.status = status;
-    tr.end_i = (uint32_t)ei;
-    tr.end_j = (uint32_t)ej;
-    tr.text_start = (uint32_t)text_start;
-    tr.n_ops = status == 0 ? n_ops : 0;
-    a.tres[jid] = tr;
-  }
-}
-
 // Sets cell c of the lane to NEG (a jump to the one cell, not a scan over all of them).
 template <int C>
 __device__ __forceinline__ void set_neg(int32_t (&h)[C], int32_t (&f)[C], int c) {
@@ -720,7 +400,7 @@ __device__ void pair_regs(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   Book b;
   bool stopped = false;
   uint32_t pw = 0;
-  uint32_t* tbp = TB ? a.tb + x.J.tb_word + lane : nullptr;
+  uint2* tbp = TB ? reinterpret_cast<uint2*>(a.tb + x.J.tb_word) + lane : nullptr;
   for (int32_t i = 1; i <= m; ++i) {
     int32_t lo, hi;
     g.range(i, lo, hi);
@@ -746,9 +426,10 @@ __device__ void pair_regs(const sfk::AffLaunch& a, uint32_t jid, int lane) {
                             lane, tbw, ecarry, xlast);
     if (W < 32 * C && lane == W / C) set_neg(h, f, W - kb);
     if constexpr (TB) {
+      constexpr int TG = CW / 2;
 #pragma unroll
-      for (int q = 0; q < CW; ++q) tbp[q * 32] = tbw[q];
-      tbp += CW * 32;
+      for (int q = 0; q < TG; ++q) tbp[q * 32] = make_uint2(tbw[q], tbw[TG + q]);
+      tbp += TG * 32;
     }
     b.cells += (uint64_t)(W > 0 ? W : 0);
     b.rows += 1;
@@ -811,9 +492,9 @@ __device__ void pair_regs(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   }
   if (lane == 0) a.out[jid] = r;
   if constexpr (TB) {
-    // __syncwarp orders the lanes' nibble stores before the walk reads them.
+    // __syncwarp orders the lanes' traceback stores before the walk reads them.
     __syncwarp();
-    walk_warp<C>(a, jid, x, g, r, lane);
+    walk_lean(a, jid, tb_layout<C>(false, false, x.J, x.P.flags), x.J, x.P.flags, r, lane);
   }
   __syncwarp();
 }
@@ -926,9 +607,11 @@ __device__ void pair_wide(const sfk::AffLaunch& a, uint32_t jid, int lane, int32
         nf[at] = f[c];
       }
       if constexpr (TB) {
-        uint32_t* dst = a.tb + x.J.tb_word + (uint64_t)(i - 1) * tb_stride + (uint64_t)q * CW * 32;
+        constexpr int TG = CW / 2;
+        uint2* dst = reinterpret_cast<uint2*>(a.tb + x.J.tb_word + (uint64_t)(i - 1) * tb_stride) +
+                     (uint64_t)q * TG * 32;
 #pragma unroll
-        for (int w = 0; w < CW; ++w) dst[w * 32 + lane] = tbw[w];
+        for (int w = 0; w < TG; ++w) dst[w * 32 + lane] = make_uint2(tbw[w], tbw[TG + w]);
       }
       if (x.rowmax_on) {
         const int32_t cm = __reduce_max_sync(FULL, lane_max(h));
@@ -1013,13 +696,10 @@ __device__ void pair_wide(const sfk::AffLaunch& a, uint32_t jid, int lane, int32
     r.cut_score = (x.cuton && plo <= (int64_t)x.J.cut) ? cutm : NEG;
   }
   __syncwarp();
-  if (lane == 0) {
-    a.out[jid] = r;
-    if constexpr (TB) {
-      const Geo32 g32{(x.P.flags & F_FULL) != 0, LOCAL, clamp30(x.J.below), clamp30(x.J.above),
-                      (int32_t)x.n};
-      walk_pass<C, true>(a, jid, x, g32, r);
-    }
+  if (lane == 0) a.out[jid] = r;
+  if constexpr (TB) {
+    __syncwarp();
+    walk_lean(a, jid, tb_layout<C>(true, false, x.J, x.P.flags), x.J, x.P.flags, r, lane);
   }
   __syncwarp();
 }

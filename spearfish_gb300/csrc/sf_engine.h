@@ -95,7 +95,8 @@ struct PinBuf {
 
 // ---- passes ----------------------------------------------------------------------------
 
-enum PassKind : uint8_t { PK_MYERS = 0, PK_AFFINE = 1, PK_LOCAL = 2 };
+// PK_AFFINE16 only classifies buckets: an affine pass the packed 16-bit kernel runs.
+enum PassKind : uint8_t { PK_MYERS = 0, PK_AFFINE = 1, PK_LOCAL = 2, PK_AFFINE16 = 3 };
 
 // One DP pass as the reference's `affine_dp` / `distance` / `local_band_core` receive it.
 struct Pass {

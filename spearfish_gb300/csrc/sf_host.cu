@@ -2,6 +2,7 @@
 // bucketing, HBM layout, persistent launches captured in a CUDA graph) and the one-call
 // entry points that mirror crates/map/src/align.rs.
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -63,6 +64,43 @@ int choose_affine_class(int64_t wmax, int& c, bool& wide) {
   c = sfk::kWideC;
   wide = true;
   return SF_OK;
+}
+
+// Whether a banded pass runs on the packed 16-bit kernel (sf_affine16_impl.cuh): Global or
+// Prefix rows of a finite band with non-negative scores, whose reachable values all stay within
+// 16384 below the row maximum the kernel rebases to every 64 rows -- the band's spread
+// (mat + ext) * width + go, 64 rows of drift of the maximum either way, and a step of slack --
+// and whose rows fit the widest 16-bit class.  SF_AFFINE16=0 in the environment turns the
+// 16-bit kernel off (every pass then runs on the 32-bit kernel).
+bool fits16(const Pass& p, uint32_t flags, int64_t wmax) {
+  if (p.kind != PK_AFFINE || (flags & F_FULL) || p.mode == SF_INFIX) return false;
+  const sf_affine_t& s = p.sc;
+  if (s.mat < 0 || s.mis < 0 || s.open < 0 || s.ext < 0) return false;
+  if (s.mat > 1000 || s.mis > 1000 || s.open > 1000 || s.ext > 1000) return false;
+  if (wmax > 32 * (int64_t)sfk::kAffine16C[sfk::kAffine16NC - 1]) return false;
+  const int64_t go = (int64_t)s.open + s.ext;
+  const int64_t step = std::max<int64_t>({(int64_t)s.mat, (int64_t)s.mis, go});
+  const int64_t spread = ((int64_t)s.mat + s.ext) * wmax + go;
+  if (spread + 2 * 64 * step + 2 * (go + s.mis + s.ext) + s.mat + 256 > 16384) return false;
+  const char* env = std::getenv("SF_AFFINE16");
+  return !(env && env[0] == '0');
+}
+
+// Kernel class of an affine or local pass: the packed 16-bit kernel when the pass fits it,
+// else the 32-bit register kernel, else (rows wider than 32 * 48 cells) the wide-row kernel.
+void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, PassKind& kind, int& c,
+                     bool& wide) {
+  wide = false;
+  if (fits16(p, flags, wmax)) {
+    for (int q = 0; q < sfk::kAffine16NC; ++q)
+      if (32 * (int64_t)sfk::kAffine16C[q] >= wmax) {
+        kind = PK_AFFINE16;
+        c = sfk::kAffine16C[q];
+        return;
+      }
+  }
+  kind = p.kind == PK_LOCAL ? PK_LOCAL : PK_AFFINE;
+  choose_affine_class(wmax, c, wide);
 }
 
 int choose_myers_class(uint32_t m, int& b, int& lanes) {
@@ -154,7 +192,7 @@ int plan_build(sf_plan* P) {
   std::vector<DJob> dj;
   std::vector<DParams> dp;
   std::vector<TJob> tj;
-  std::vector<uint8_t> cls;
+  std::vector<uint16_t> cls;
   std::vector<MJob> mj;
   std::vector<uint32_t> wlist;
   P->slot.assign(np, 0);
@@ -200,7 +238,8 @@ int plan_build(sf_plan* P) {
     const int64_t wmax = band_wmax(j, flags);
     int c = 4;
     bool wide = false;
-    choose_affine_class(wmax, c, wide);
+    PassKind kind = PK_AFFINE;
+    classify_affine(p, flags, wmax, kind, c, wide);
     const bool tb = p.want_cigar && p.kind != PK_LOCAL;
     if (tb) {
       flags |= F_TB;
@@ -230,12 +269,11 @@ int plan_build(sf_plan* P) {
     }
     P->slot[q] = (uint32_t)dj.size();
     const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
-    items.push_back({Key2{p.kind == PK_LOCAL ? PK_LOCAL : PK_AFFINE, c, wide, tb, 32},
-                     Item{(uint32_t)dj.size(), work}});
+    items.push_back({Key2{kind, c, wide, tb, 32}, Item{(uint32_t)dj.size(), work}});
     dj.push_back(j);
     dp.push_back(pr);
     tj.push_back(t);
-    cls.push_back((uint8_t)(wide ? (0x80 | c) : c));
+    cls.push_back((uint16_t)(c | (wide ? 0x100 : 0) | (kind == PK_AFFINE16 ? 0x200 : 0)));
   }
   P->n_aff = (uint32_t)dj.size();
   P->n_my = (uint32_t)mj.size();
@@ -304,7 +342,7 @@ int plan_build(sf_plan* P) {
   if ((rc = P->d_res.ensure(dj.size() * sizeof(DRes) + 64))) return rc;
   if ((rc = P->d_tjobs.ensure(tj.size() * sizeof(TJob) + 64))) return rc;
   if ((rc = P->d_tres.ensure(tj.size() * sizeof(TRes) + 64))) return rc;
-  if ((rc = P->d_cls.ensure(cls.size() + 64))) return rc;
+  if ((rc = P->d_cls.ensure(cls.size() * 2 + 64))) return rc;
   if ((rc = P->d_mjobs.ensure(mj.size() * sizeof(MJob) + 64))) return rc;
   if ((rc = P->d_mout.ensure(mj.size() * 4 + 64))) return rc;
   if ((rc = P->d_tb.ensure(tb_words * 4 + 64))) return rc;
@@ -341,7 +379,7 @@ int plan_build(sf_plan* P) {
   if ((rc = put(P->d_djobs, dj.data(), dj.size() * sizeof(DJob)))) return rc;
   if ((rc = put(P->d_params, dp.data(), dp.size() * sizeof(DParams)))) return rc;
   if ((rc = put(P->d_tjobs, tj.data(), tj.size() * sizeof(TJob)))) return rc;
-  if ((rc = put(P->d_cls, cls.data(), cls.size()))) return rc;
+  if ((rc = put(P->d_cls, cls.data(), cls.size() * 2))) return rc;
   if ((rc = put(P->d_mjobs, mj.data(), mj.size() * sizeof(MJob)))) return rc;
   if ((rc = put(P->d_order, order.data(), order.size() * 4))) return rc;
   if ((rc = put(P->d_wlist, wlist.data(), wlist.size() * 4))) return rc;
@@ -361,7 +399,11 @@ int plan_build(sf_plan* P) {
     std::snprintf(buf, sizeof buf,
                   "%s{\"kind\": \"%s\", \"c\": %d, \"wide\": %s, \"traceback\": %s, \"lanes\": %d, "
                   "\"jobs\": %u, \"grid\": %d, \"block\": %d, \"work\": %llu}",
-                  q ? ", " : "", b.kind == PK_MYERS ? "myers" : (b.kind == PK_LOCAL ? "local" : "affine"), b.c,
+                  q ? ", " : "",
+                  b.kind == PK_MYERS ? "myers"
+                                     : (b.kind == PK_LOCAL ? "local"
+                                                           : (b.kind == PK_AFFINE16 ? "affine16" : "affine")),
+                  b.c,
                   b.wide ? "true" : "false", b.tb ? "true" : "false", b.lanes, b.count, b.grid,
                   b.block, (unsigned long long)bwork[q]);
     d += buf;
@@ -440,7 +482,10 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
       al.tjobs = P->d_tjobs.as<TJob>();
       al.ops = P->d_ops.as<uint32_t>();
       al.tres = P->d_tres.as<TRes>();
-      CK(sfk::launch_affine(b.c, b.wide, b.tb, b.kind == PK_LOCAL, al, b.grid, b.block, bs));
+      if (b.kind == PK_AFFINE16)
+        CK(sfk::launch_affine16(b.c, b.tb, al, b.grid, b.block, bs));
+      else
+        CK(sfk::launch_affine(b.c, b.wide, b.tb, b.kind == PK_LOCAL, al, b.grid, b.block, bs));
     }
     launches++;
     if ((mrc = mark())) return mrc;
@@ -452,7 +497,7 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
     }
   }
   if (P->n_walk) {
-    // The passes walked their own paths (fused into the affine kernels); compact the CIGARs.
+    // The passes walked their own paths (sf_walk.cuh); compact the CIGARs.
     CK(sfk::launch_compact(P->d_tres.as<TRes>(), P->d_tjobs.as<TJob>(), P->d_wlist.as<uint32_t>(),
                            P->n_walk, P->d_offs.as<uint64_t>(), P->d_ops.as<uint32_t>(),
                            P->d_opsc.as<uint32_t>(), P->d_total.as<uint64_t>(), s));
@@ -812,7 +857,8 @@ uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_byte
     const int64_t wmax = band_wmax(j, flags);
     int c = 4;
     bool wide = false;
-    choose_affine_class(wmax, c, wide);
+    PassKind kind = PK_AFFINE;
+    classify_affine(p, flags, wmax, kind, c, wide);
     if (p.want_cigar && p.kind != PK_LOCAL) {
       b += (uint64_t)p.m * tb_row_words(c, wide ? wide_chunks(c, wmax) : 1) * 4;
       b += 2 * ((uint64_t)p.m + p.n + 2) * 4;

@@ -76,7 +76,8 @@ struct TRes {
   uint32_t end_i, end_j, text_start, n_ops;
 };
 
-// Traceback words per lane and row: two bit-plane words per group of 16 cells.
+// Traceback words per lane and row: two bit-plane words per group of 16 cells, stored as one
+// 8-byte pair (A, B) per lane and group, lane-fastest: pair g*32 + lane of the row.
 __host__ __device__ inline uint32_t tb_words_per_lane(int c) { return (uint32_t)(2 * ((c + 15) / 16)); }
 
 // The widest row of a pass: banded rows are at most below + above + 1 cells
@@ -154,6 +155,11 @@ cudaError_t launch_affine(int c, bool wide, bool tb, bool local, const AffLaunch
 extern const int kAffineC[];
 extern const int kAffineNC;
 constexpr int kWideC = 16;
+// Packed 16-bit register kernel (two cells per register): C cells per lane, even.
+cudaError_t launch_affine16(int c, bool tb, const AffLaunch& a, int grid, int block,
+                            cudaStream_t s);
+extern const int kAffine16C[];
+extern const int kAffine16NC;
 
 
 struct MyersLaunch {

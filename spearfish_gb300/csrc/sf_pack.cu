@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(256) gather_kernel(const sf::TRes* tres, const
     if (r.status != 0) continue;
     const uint32_t* src = in + tjobs[j].ops_off;
     uint32_t* dst = out + offs[q];
-    for (uint32_t x = lane; x < r.n_ops; x += 32) dst[x] = src[x];
+    // The walk wrote the ops end first.
+    for (uint32_t x = lane; x < r.n_ops; x += 32) dst[x] = src[r.n_ops - 1 - x];
   }
 }
 
