@@ -25,6 +25,8 @@
 // columns, which shift one column per row with the band.  Traceback decisions go out as one
 // (A, B) word pair per lane and group of 8 words; sf_walk.cuh decodes that layout.
 #pragma once
+#include <utility>
+
 #include "sf_affine_impl.cuh"
 
 namespace {
@@ -38,24 +40,29 @@ constexpr int kRebaseRows = 64;
 
 __device__ __forceinline__ uint32_t pk2(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
 
+// Calls f(std::integral_constant<int, k>) for k = 0 .. N - 1 (compile-time word indices).
+template <int N, class F, int... K>
+__device__ __forceinline__ void sf_unroll_impl(F&& f, std::integer_sequence<int, K...>) {
+  (f(std::integral_constant<int, K>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void sf_unroll(F&& f) {
+  sf_unroll_impl<N>(f, std::make_integer_sequence<int, N>{});
+}
+
 // Bit 15 / 31: the low / high field of a exceeds b's (fields within 0x7fff of each other).
 __device__ __forceinline__ uint32_t gt2(uint32_t a, uint32_t b) { return a - b + kGt2; }
 
-// Two decisions of one word into a traceback word: bytes (d1 lo, d1 hi, d2 lo, d2 hi), each
-// byte receiving the decision at bit 7 after shifting the earlier ones down.
+// Two decisions of word t (of its group of 8) into a traceback word: byte 0 / 1 receive the
+// low / high field's decision of d1 at bit t, bytes 2 / 3 those of d2.  The byte permute
+// (PTX prmt, whose selector nibbles with bit 3 set replicate the selected byte's msb; the
+// __byte_perm intrinsic uses only 3 selector bits) spreads each compare bit (bit 15 / 31)
+// over its byte, the mask keeps bit t.
+template <int T>
 __device__ __forceinline__ uint32_t push2(uint32_t acc, uint32_t d1, uint32_t d2) {
-  const uint32_t w = __byte_perm(d1, d2, 0x7531);
-  return ((acc >> 1) & 0x7f7f7f7fu) | (w & 0x80808080u);
-}
-
-// Score of each text code against the row's pattern base p, as a 16-bit field: low bytes in
-// ta, high bytes in tb, byte t for code t.
-__device__ __forceinline__ void score_tables(uint32_t p, int32_t mat, int32_t mis, uint32_t& ta,
-                                             uint32_t& tb) {
-  const uint32_t nm = (uint32_t)(-mis) & 0xffffu, mt = (uint32_t)mat & 0xffffu;
-  const uint32_t sh = 8u * (p & 3u), keep = ~(0xffu << sh);
-  ta = (((nm & 0xffu) * 0x01010101u) & keep) | ((mt & 0xffu) << sh);
-  tb = (((nm >> 8) * 0x01010101u) & keep) | ((mt >> 8) << sh);
+  uint32_t w;
+  asm("prmt.b32 %0, %1, %2, 0xFDB9;" : "=r"(w) : "r"(d1), "r"(d2));
+  return acc | (w & (0x01010101u << T));
 }
 
 // Selector byte of a text code for __byte_perm(ta, tb, .): nibbles (t, t + 4).
@@ -132,8 +139,10 @@ template <int C2, bool TB>
 __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   constexpr int C = 2 * C2;
   constexpr int G = (C2 + 7) / 8;
-  constexpr int CW = 2 * G;
-  static_assert(CW == 2 * ((C + 15) / 16), "same traceback row size as the 32-bit kernel");
+  static_assert(2 * G == 2 * ((C + 15) / 16), "same traceback row size as the 32-bit kernel");
+  // Rows of at most 8 words keep the sentinel's position as per-word masks; wider rows jump
+  // to it (a switch), short of registers for the masks.
+  constexpr bool kMasks = C2 <= 8;
   const PassCtx x = make_ctx(a, jid);
   DRes r{};
   const int32_t m = (int32_t)x.m, n = (int32_t)x.n;
@@ -147,8 +156,16 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   const uint32_t one = (uint32_t)opaque_one();
   const uint32_t go2 = (uint32_t)x.go * kOne2;
   const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;  // + (-ext) mod 2^16
+  // Score bytes: -mis and mat as 16-bit fields, low and high bytes replicated; a row's table
+  // takes byte p (its pattern base) from mat, the others from -mis.
+  const uint32_t nmis = (uint32_t)(-x.mis) & 0xffffu, mat = (uint32_t)x.mat & 0xffffu;
+  const uint32_t misA = (nmis & 0xffu) * 0x01010101u, misB = (nmis >> 8) * 0x01010101u;
+  const uint32_t matA = (mat & 0xffu) * 0x01010101u, matB = (mat >> 8) * 0x01010101u;
+  // Warp-scan decays: a lane's gap value falls by ext * C per lane it crosses.
+  const int32_t dC = x.ext * C, dH = -x.ext * C2;
+  const int32_t e_lane = (int32_t)kNeg16 - dC * lane;  // NEG at the band's left end, decayed
   int32_t off = -(int32_t)kBias16;  // value = field + off
-  uint32_t h[C2], f[C2], sel[C2];
+  uint32_t h[C2], f[C2], sel[C2], smask[kMasks ? C2 : 1];
   int32_t plo, phi;
   g.range(0, plo, phi);
   {
@@ -160,34 +177,47 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
       const uint32_t hi = K2 < w0 ? (uint32_t)(row0_value(x, plo + K2) - off) : kNeg16;
       h[k] = pk2(lo, hi);
       f[k] = kNeg2;
-      sel[k] = 0;
     }
   }
+  {
+    // Text selectors of row 1's columns; later rows shift them with the band.
+    int32_t lo1, hi1;
+    g.range(1, lo1, hi1);
+    Win<C> win;
+    win.load(a.pool, x.J.t_word, lo1 + kb);
+#pragma unroll
+    for (int k = 0; k < C2; ++k) sel[k] = sel_byte(win.at(k)) | (sel_byte(win.at(C2 + k)) << 8);
+  }
+  int32_t Wm = -1;  // the row width the sentinel masks are for
+  auto set_masks = [&](int32_t W) {
+    const int32_t c = W - kb;
+#pragma unroll
+    for (int k = 0; k < (kMasks ? C2 : 1); ++k)
+      smask[k] = (c == k ? 0xffffu : 0u) | (c == C2 + k ? 0xffff0000u : 0u);
+    Wm = W;
+  };
   Book b;
-  bool stopped = false;
-  uint32_t pw = 0;
+  uint32_t pw = m > 0 ? __ldg(a.pool + x.J.p_word) >> 2 : 0;  // pattern bases from row 1
   uint2* tbp = TB ? reinterpret_cast<uint2*>(a.tb + x.J.tb_word) + lane : nullptr;
-  for (int32_t i = 1; i <= m; ++i) {
+
+  // One row.  D1: lo moved right by one (offset K reads the previous row at K + 1 above and
+  // K diagonally); else lo stayed (K above, K - 1 diagonally; lo = 0, column 0 in lane 0).
+  // Returns true when the pass stops at this row.
+  auto row = [&](int32_t i, auto d1tag) -> bool {
+    constexpr bool D1 = decltype(d1tag)::value;
     int32_t lo, hi;
     g.range(i, lo, hi);
     if (lo > hi) {
       r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)i,
                b.rows, b.cells};
-      stopped = true;
-      break;
+      return true;
     }
-    const int d = lo - plo;
     const int32_t W = hi - lo + 1;
-    const uint32_t cpat = pattern_code(a, x, i, pw);
-    uint32_t ta, tbl;
-    score_tables(cpat, x.mat, x.mis, ta, tbl);
-    // Selectors of this row's text columns: loaded at row 1, then shifted with the band.
-    if (i == 1) {
-      Win<C> win;
-      win.load(a.pool, x.J.t_word, lo + kb);
-#pragma unroll
-      for (int k = 0; k < C2; ++k) sel[k] = sel_byte(win.at(k)) | (sel_byte(win.at(C2 + k)) << 8);
-    } else if (d) {
+    if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + (i >> 4));
+    const uint32_t selp = 0x3210u + (4u << (4u * (pw & 3u)));
+    pw >>= 2;
+    const uint32_t ta = __byte_perm(misA, matA, selp), tbl = __byte_perm(misB, matB, selp);
+    if (D1 && i > 1) {
       const uint32_t s0 = sel[0];
       uint32_t nx = __shfl_down_sync(FULL, s0, 1);
       const uint32_t far = sel_byte(base_at(a.pool, x.J.t_word, (uint64_t)(lo + 32 * C - 1)));
@@ -202,50 +232,54 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
     uint32_t acc1[G];
 #pragma unroll
     for (int q = 0; q < G; ++q) acc1[q] = 0;
-    auto cell = [&](int k, uint32_t hd, uint32_t hu, uint32_t fu) {
+    auto cell = [&](auto kt, uint32_t hd, uint32_t hu, uint32_t fu) {
+      constexpr int k = decltype(kt)::value;
       const uint32_t ho = hu * one - go2;
       const uint32_t fo = __viaddmax_u16x2(fu, next2, kNeg2);
       const uint32_t fj = __vmaxu2(ho, fo);
       const uint32_t s2 = __byte_perm(ta, tbl, sel[k]);
       const uint32_t dg = __viaddmax_u16x2(hd, s2, 0u);
       const uint32_t xx = __vmaxu2(dg, fj);
-      if constexpr (TB) acc1[k >> 3] = push2(acc1[k >> 3], gt2(fj, ho), gt2(xx, dg));
+      if constexpr (TB) acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), gt2(xx, dg));
       chain = __viaddmax_u16x2(chain, next2, xx * one - go2);
       f[k] = fj;
       h[k] = xx;
     };
-    if (d) {
+    if constexpr (D1) {
       uint32_t nH = __shfl_down_sync(FULL, h[0], 1), nF = __shfl_down_sync(FULL, f[0], 1);
       if (lane == 31) nH = nF = kNeg2;
       const uint32_t upH = __byte_perm(h[0], nH, 0x5432), upF = __byte_perm(f[0], nF, 0x5432);
-#pragma unroll
-      for (int k = 0; k < C2; ++k)
-        cell(k, h[k], k + 1 < C2 ? h[k + 1] : upH, k + 1 < C2 ? f[k + 1] : upF);
+      sf_unroll<C2>([&](auto kt) {
+        constexpr int k = decltype(kt)::value;
+        cell(kt, h[k], k + 1 < C2 ? h[k + 1 < C2 ? k + 1 : 0] : upH,
+             k + 1 < C2 ? f[k + 1 < C2 ? k + 1 : 0] : upF);
+      });
     } else {
-      // d = 0 only while lo = 0: lane 0's first cell is column 0, reached by a vertical gap
-      // alone (align.rs:2558-2566); its diagonal gets a field no F can lose to.
+      // Lane 0's first cell is column 0, reached by a vertical gap alone
+      // (align.rs:2558-2566); its diagonal gets a field no F can lose to.
       const uint32_t pl = __shfl_up_sync(FULL, h[C2 - 1], 1);
       uint32_t hd = __byte_perm(pl, h[C2 - 1], 0x5432);
       if (lane == 0) hd = (hd & 0xffff0000u) | (kNeg16 - (uint32_t)x.mat - 1u);
-#pragma unroll
-      for (int k = 0; k < C2; ++k) {
+      sf_unroll<C2>([&](auto kt) {
+        constexpr int k = decltype(kt)::value;
         const uint32_t hu = h[k];
-        cell(k, hd, hu, f[k]);
+        cell(kt, hd, hu, f[k]);
         hd = hu;
-      }
+      });
     }
 
     // Gap entering each lane (32-bit fields): the lane's chain leaves its low half decayed
     // by ext * C/2 and meets its high half's.
     const int32_t clo = (int32_t)(chain & 0xffffu), chi = (int32_t)(chain >> 16);
-    const int32_t dC = x.ext * C;
-    int32_t S = addmax(clo, -x.ext * C2, chi);
-#pragma unroll
-    for (int sft = 1; sft < 32; sft <<= 1)
-      S = addmax(__shfl_up_sync(FULL, S, sft), -dC * sft, S);
+    int32_t S = addmax(clo, dH, chi);
+    S = addmax(__shfl_up_sync(FULL, S, 1), -dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 2), -2 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 4), -4 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 8), -8 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 16), -16 * dC, S);
     const int32_t Sp = __shfl_up_sync(FULL, S, 1);
-    const int32_t ein = lane == 0 ? (int32_t)kNeg16 : addmax((int32_t)kNeg16, -dC * lane, Sp);
-    const int32_t ehi = addmax(ein, -x.ext * C2, clo);
+    const int32_t ein = lane == 0 ? (int32_t)kNeg16 : max(e_lane, Sp);
+    const int32_t ehi = addmax(ein, dH, clo);
     uint32_t e = pk2((uint32_t)ein, (uint32_t)ehi);
     // H' left of each half's first cell (lane 0: none -- a field below NEG, so that lane 0's
     // entering E, NEG, counts as extended whatever go is, as in the 32-bit kernel).
@@ -257,15 +291,15 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
     uint32_t acc2[G];
 #pragma unroll
     for (int q = 0; q < G; ++q) acc2[q] = 0;
-#pragma unroll
-    for (int k = 0; k < C2; ++k) {
+    sf_unroll<C2>([&](auto kt) {
+      constexpr int k = decltype(kt)::value;
       const uint32_t xx = h[k];
       const uint32_t xo = xp * one - go2;
       if (k > 0) e = __viaddmax_u16x2(e, next2, xo);
-      if constexpr (TB) acc2[k >> 3] = push2(acc2[k >> 3], gt2(e, xo), gt2(e, xx));
+      if constexpr (TB) acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], gt2(e, xo), gt2(e, xx));
       h[k] = __vmaxu2(xx, e);
       xp = xx;
-    }
+    });
     if constexpr (TB) {
 #pragma unroll
       for (int q = 0; q < G; ++q) tbp[q * 32] = make_uint2(acc1[q], acc2[q]);
@@ -279,9 +313,10 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
       if (x.rowmax_on) {
         const int32_t rmax = (int32_t)rmu + off;
         if (x.cuton && lo <= cut) {
-          int32_t row = rmax;
-          if (hi > cut) row = (int32_t)__reduce_max_sync(FULL, lane_max16(h, kb, cut - lo + 1)) + off;
-          b.cut_best = max(b.cut_best, row);
+          int32_t rowv = rmax;
+          if (hi > cut)
+            rowv = (int32_t)__reduce_max_sync(FULL, lane_max16(h, kb, cut - lo + 1)) + off;
+          b.cut_best = max(b.cut_best, rowv);
         }
         if (x.clip) {
           if (rmax > b.clip_best) {
@@ -292,10 +327,9 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
             }
           }
           if (rmax < sat_sub(b.clip_best, x.P.xdrop)) {
-            r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)hi, (uint32_t)i,
-                     b.rows, b.cells};
-            stopped = true;
-            break;
+            r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)hi,
+                     (uint32_t)i, b.rows, b.cells};
+            return true;
           }
         }
       }
@@ -311,10 +345,28 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
       }
     }
     // The sentinel right of the band (align.rs:2490-2494), after any rebase.
-    if (W < 32 * C && lane == W / C) set_neg16(h, f, W - kb);
+    if (W < 32 * C) {
+      if constexpr (kMasks) {
+        if (W != Wm) set_masks(W);
+#pragma unroll
+        for (int k = 0; k < C2; ++k) {
+          h[k] = (h[k] & ~smask[k]) | (kNeg2 & smask[k]);
+          f[k] = (f[k] & ~smask[k]) | (kNeg2 & smask[k]);
+        }
+      } else if (lane == W / C) {
+        set_neg16(h, f, W - kb);
+      }
+    }
     plo = lo;
     phi = hi;
-  }
+    return false;
+  };
+
+  // Rows 1 .. below keep lo = 0 (align.rs:2462-2468); later rows move it right by one.
+  bool stopped = false;
+  const int32_t endA = m < g.below ? m : g.below;
+  for (int32_t i = 1; i <= endA && !stopped; ++i) stopped = row(i, std::false_type{});
+  for (int32_t i = endA + 1; i <= m && !stopped; ++i) stopped = row(i, std::true_type{});
   if (!stopped) {
     const int32_t W = phi - plo + 1;
     r.clip_best = b.clip_best;
@@ -351,7 +403,7 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
 
 template <int C2>
 struct MinBlocks16 {
-  static constexpr int value = C2 <= 8 ? 6 : (C2 <= 14 ? 5 : (C2 <= 16 ? 4 : (C2 <= 24 ? 3 : 2)));
+  static constexpr int value = C2 <= 8 ? 6 : (C2 <= 10 ? 4 : (C2 <= 16 ? 3 : 2));
 };
 
 template <int C2, bool TB>

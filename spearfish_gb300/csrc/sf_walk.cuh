@@ -59,8 +59,7 @@ struct TbLayout {
     if (p16) {
       const int hi = p.c >= C2, k = hi ? p.c - C2 : p.c;
       const int g = k >> 3, t = k & 7;
-      const int gs = (C2 - 8 * g) < 8 ? (C2 - 8 * g) : 8;
-      sh = 8 * hi + 8 - gs + t;
+      sh = 8 * hi + t;
       return g * 32 + p.L;
     }
     const int g = p.c >> 4, q = p.c & 15;
