@@ -135,6 +135,25 @@ __device__ __forceinline__ void set_neg16(uint32_t (&h)[C2], uint32_t (&f)[C2], 
   static_assert(C2 <= 32, "set_neg16 covers 32 words per lane");
 }
 
+// DP_WORK cells of rows 1 .. R of a banded pass (align.rs:2573-2578): the sum of
+// hi_i - lo_i + 1 with lo_i = max(0, i - below), hi_i = min(i + above, n), rows whose band is
+// not empty.
+__device__ __forceinline__ uint64_t band_cells(int64_t R, int64_t below, int64_t above,
+                                               int64_t n) {
+  if (R <= 0) return 0;
+  const int64_t t = n - above;  // rows with i + above <= n
+  int64_t s1;                   // sum of hi_i
+  if (t >= R)
+    s1 = R * (R + 1) / 2 + R * above;
+  else if (t < 1)
+    s1 = R * n;
+  else
+    s1 = t * (t + 1) / 2 + t * above + (R - t) * n;
+  const int64_t u = R - below;  // rows with lo_i > 0
+  const int64_t s2 = u > 0 ? u * (u + 1) / 2 : 0;
+  return (uint64_t)(s1 - s2 + R);
+}
+
 template <int C2, bool TB>
 __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   constexpr int C = 2 * C2;
@@ -156,13 +175,17 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   const uint32_t one = (uint32_t)opaque_one();
   const uint32_t go2 = (uint32_t)x.go * kOne2;
   const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;  // + (-ext) mod 2^16
-  // Score bytes: -mis and mat as 16-bit fields, low and high bytes replicated; a row's table
-  // takes byte p (its pattern base) from mat, the others from -mis.
-  const uint32_t nmis = (uint32_t)(-x.mis) & 0xffffu, mat = (uint32_t)x.mat & 0xffffu;
-  const uint32_t misA = (nmis & 0xffu) * 0x01010101u, misB = (nmis >> 8) * 0x01010101u;
-  const uint32_t matA = (mat & 0xffu) * 0x01010101u, matB = (mat >> 8) * 0x01010101u;
-  // Warp-scan decays: a lane's gap value falls by ext * C per lane it crosses.
+  const uint32_t ext2 = (uint32_t)x.ext * kOne2;
+  // Match scores enter as s + mis (mat + mis or 0, so that a plain add of both fields cannot
+  // borrow); the maximum that takes the diagonal subtracts mis again.  A row's table holds
+  // mat + mis in byte p (its pattern base) of ta (low bytes) and tb (high bytes), 0 elsewhere.
+  const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
+  const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
+  const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;  // gt2 against diagonal + mis
+  // Warp-scan decays: a lane's gap value falls by ext * C per lane it crosses.  The lane's
+  // own chain is the maximum over its cells of H' + ext * k, less go + ext * (C/2 - 1).
   const int32_t dC = x.ext * C, dH = -x.ext * C2;
+  const int32_t goX = x.go + x.ext * (C2 - 1);
   const int32_t e_lane = (int32_t)kNeg16 - dC * lane;  // NEG at the band's left end, decayed
   int32_t off = -(int32_t)kBias16;  // value = field + off
   uint32_t h[C2], f[C2], sel[C2], smask[kMasks ? C2 : 1];
@@ -205,18 +228,13 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   // Returns true when the pass stops at this row.
   auto row = [&](int32_t i, auto d1tag) -> bool {
     constexpr bool D1 = decltype(d1tag)::value;
-    int32_t lo, hi;
-    g.range(i, lo, hi);
-    if (lo > hi) {
-      r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)i,
-               b.rows, b.cells};
-      return true;
-    }
+    // align.rs:2462-2468; rows past n + below (empty) never get here.
+    const int32_t lo = D1 ? i - g.below : 0, hi = min(i + g.above, n);
     const int32_t W = hi - lo + 1;
     if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + (i >> 4));
-    const uint32_t selp = 0x3210u + (4u << (4u * (pw & 3u)));
+    const uint32_t pb = 8u * (pw & 3u);
     pw >>= 2;
-    const uint32_t ta = __byte_perm(misA, matA, selp), tbl = __byte_perm(misB, matB, selp);
+    const uint32_t ta = (mpm & 0xffu) << pb, tbl = (mpm >> 8) << pb;
     if (D1 && i > 1) {
       const uint32_t s0 = sel[0];
       uint32_t nx = __shfl_down_sync(FULL, s0, 1);
@@ -227,21 +245,29 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
       sel[C2 - 1] = __byte_perm(s0, nx, 0x2241);  // (old word 0 high column, next lane's low)
     }
 
-    // Pass 1: F, H' and the lane's horizontal-gap chain.
-    uint32_t chain = kNeg2;
+    // Pass 1: F, H' and the lane's horizontal-gap chain.  F = max(Hup - go, Fup - ext): the
+    // 32-bit kernel's floor at NEG only ever lifts values that lose to a reachable one, so
+    // it is left out (F above the band's sentinel sits ext below NEG instead of at it).
+    uint32_t red = 0, pend = 0;  // maximum of H' + ext * k over the lane's words
     uint32_t acc1[G];
 #pragma unroll
     for (int q = 0; q < G; ++q) acc1[q] = 0;
     auto cell = [&](auto kt, uint32_t hd, uint32_t hu, uint32_t fu) {
       constexpr int k = decltype(kt)::value;
       const uint32_t ho = hu * one - go2;
-      const uint32_t fo = __viaddmax_u16x2(fu, next2, kNeg2);
+      const uint32_t fo = fu * one - ext2;
       const uint32_t fj = __vmaxu2(ho, fo);
-      const uint32_t s2 = __byte_perm(ta, tbl, sel[k]);
-      const uint32_t dg = __viaddmax_u16x2(hd, s2, 0u);
-      const uint32_t xx = __vmaxu2(dg, fj);
-      if constexpr (TB) acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), gt2(xx, dg));
-      chain = __viaddmax_u16x2(chain, next2, xx * one - go2);
+      const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);  // diagonal + s + mis
+      const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
+      if constexpr (TB)
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), xx - dgp + kGtDg);
+      const uint32_t t = ext2 * (uint32_t)k + xx;
+      if constexpr (k == 0)
+        red = t;
+      else if constexpr (k & 1)
+        pend = t;
+      else
+        red = __vimax3_u16x2(red, pend, t);
       f[k] = fj;
       h[k] = xx;
     };
@@ -268,9 +294,10 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
       });
     }
 
+    if constexpr (C2 % 2 == 0) red = __vmaxu2(red, pend);
     // Gap entering each lane (32-bit fields): the lane's chain leaves its low half decayed
     // by ext * C/2 and meets its high half's.
-    const int32_t clo = (int32_t)(chain & 0xffffu), chi = (int32_t)(chain >> 16);
+    const int32_t clo = (int32_t)(red & 0xffffu) - goX, chi = (int32_t)(red >> 16) - goX;
     int32_t S = addmax(clo, dH, chi);
     S = addmax(__shfl_up_sync(FULL, S, 1), -dC, S);
     S = addmax(__shfl_up_sync(FULL, S, 2), -2 * dC, S);
@@ -305,8 +332,6 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
       for (int q = 0; q < G; ++q) tbp[q * 32] = make_uint2(acc1[q], acc2[q]);
       tbp += G * 32;
     }
-    b.cells += (uint64_t)W;
-    b.rows += 1;
     const bool rebase = (i & (kRebaseRows - 1)) == 0;
     if (x.rowmax_on || rebase) {
       const uint32_t rmu = __reduce_max_sync(FULL, lane_max16(h, kb, W));
@@ -328,7 +353,7 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
           }
           if (rmax < sat_sub(b.clip_best, x.P.xdrop)) {
             r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)hi,
-                     (uint32_t)i, b.rows, b.cells};
+                     (uint32_t)i, (uint32_t)i, band_cells(i, g.below, g.above, n)};
             return true;
           }
         }
@@ -365,8 +390,16 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   // Rows 1 .. below keep lo = 0 (align.rs:2462-2468); later rows move it right by one.
   bool stopped = false;
   const int32_t endA = m < g.below ? m : g.below;
+  const int64_t lastB = (int64_t)n + g.below;  // the last row whose band is not empty
+  const int32_t endB = (int64_t)m < lastB ? m : (int32_t)lastB;
   for (int32_t i = 1; i <= endA && !stopped; ++i) stopped = row(i, std::false_type{});
-  for (int32_t i = endA + 1; i <= m && !stopped; ++i) stopped = row(i, std::true_type{});
+  for (int32_t i = endA + 1; i <= endB && !stopped; ++i) stopped = row(i, std::true_type{});
+  if (!stopped && endB < m) {
+    // Row endB + 1 lies past the text: the pass ends there with no score (align.rs:2543-2553).
+    r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)(endB + 1),
+             (uint32_t)endB, band_cells(endB, g.below, g.above, n)};
+    stopped = true;
+  }
   if (!stopped) {
     const int32_t W = phi - plo + 1;
     r.clip_best = b.clip_best;
@@ -375,8 +408,8 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
     r.clip_j = b.cj;
     r.text_read = (uint32_t)phi;
     r.last_row = (uint32_t)m;
-    r.rows = b.rows;
-    r.cells = b.cells;
+    r.rows = (uint32_t)m;
+    r.cells = band_cells(m, g.below, g.above, n);
     if (x.mode == 2) {
       const int32_t K = n - plo;
       const uint32_t u = __shfl_sync(FULL, field_at(h, K % C), (K / C) & 31);
