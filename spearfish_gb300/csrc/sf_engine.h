@@ -148,7 +148,7 @@ struct sf_plan {
   DevBuf d_bytes, d_pool, d_seq, d_djobs, d_params, d_res, d_mjobs, d_mout, d_tjobs, d_tres,
       d_tb, d_ops, d_opsc, d_offs, d_order, d_counters, d_wlist, d_cls, d_scratch, d_total;
   // Pinned staging.
-  PinBuf h_stage, h_res, h_mout, h_tres, h_ops;
+  PinBuf h_stage, h_res, h_mout, h_tres, h_ops, h_total;
   cudaGraphExec_t graph = nullptr;
   bool graph_tried = false;
   uint64_t launches = 0;
@@ -197,7 +197,7 @@ int plan_fetch(sf_plan* P);
 int plan_fetch_ops(sf_plan* P, uint64_t& total);
 // Converts a fetched plan's results to sf_result_t (and copies compacted ops).
 int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
-                 uint64_t total);
+                 uint64_t total, bool copy_ops = true);
 // Device bytes a plan of these passes needs (upper bound, before building it).
 uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_bytes);
 // Device bytes the plan's buffers hold now.

@@ -70,8 +70,7 @@ int choose_affine_class(int64_t wmax, int& c, bool& wide) {
 // Prefix rows of a finite band with non-negative scores, whose reachable values all stay within
 // 16384 below the row maximum the kernel rebases to every 64 rows -- the band's spread
 // (mat + ext) * width + go, 64 rows of drift of the maximum either way, and a step of slack --
-// and whose rows fit the widest 16-bit class.  SF_AFFINE16=0 in the environment turns the
-// 16-bit kernel off (every pass then runs on the 32-bit kernel).
+// and whose rows fit the widest 16-bit class.
 bool fits16(const Pass& p, uint32_t flags, int64_t wmax) {
   if (p.kind != PK_AFFINE || (flags & F_FULL) || p.mode == SF_INFIX) return false;
   const sf_affine_t& s = p.sc;
@@ -81,17 +80,22 @@ bool fits16(const Pass& p, uint32_t flags, int64_t wmax) {
   const int64_t go = (int64_t)s.open + s.ext;
   const int64_t step = std::max<int64_t>({(int64_t)s.mat, (int64_t)s.mis, go});
   const int64_t spread = ((int64_t)s.mat + s.ext) * wmax + go;
-  if (spread + 2 * 64 * step + 2 * (go + s.mis + s.ext) + s.mat + 256 > 16384) return false;
+  return spread + 2 * 64 * step + 2 * (go + s.mis + s.ext) + s.mat + 256 <= 16384;
+}
+
+// SF_AFFINE16=0 in the environment turns the 16-bit kernel off (every pass then runs on the
+// 32-bit kernel); read once per plan.
+bool allow16() {
   const char* env = std::getenv("SF_AFFINE16");
   return !(env && env[0] == '0');
 }
 
 // Kernel class of an affine or local pass: the packed 16-bit kernel when the pass fits it,
 // else the 32-bit register kernel, else (rows wider than 32 * 48 cells) the wide-row kernel.
-void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, PassKind& kind, int& c,
-                     bool& wide) {
+void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, PassKind& kind,
+                     int& c, bool& wide) {
   wide = false;
-  if (fits16(p, flags, wmax)) {
+  if (use16 && fits16(p, flags, wmax)) {
     for (int q = 0; q < sfk::kAffine16NC; ++q)
       if (32 * (int64_t)sfk::kAffine16C[q] >= wmax) {
         kind = PK_AFFINE16;
@@ -194,6 +198,10 @@ int plan_build(sf_plan* P) {
   std::vector<TJob> tj;
   std::vector<uint16_t> cls;
   std::vector<MJob> mj;
+  dj.reserve(np);
+  dp.reserve(np);
+  tj.reserve(np);
+  cls.reserve(np);
   std::vector<uint32_t> wlist;
   P->slot.assign(np, 0);
   struct Item {
@@ -211,6 +219,7 @@ int plan_build(sf_plan* P) {
   };
   std::vector<std::pair<Key2, Item>> items;
   items.reserve(np);
+  const bool use16 = allow16();
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
@@ -239,7 +248,7 @@ int plan_build(sf_plan* P) {
     int c = 4;
     bool wide = false;
     PassKind kind = PK_AFFINE;
-    classify_affine(p, flags, wmax, kind, c, wide);
+    classify_affine(p, flags, wmax, use16, kind, c, wide);
     const bool tb = p.want_cigar && p.kind != PK_LOCAL;
     if (tb) {
       flags |= F_TB;
@@ -282,30 +291,66 @@ int plan_build(sf_plan* P) {
   P->ops_words = ops_words;
   P->scratch_cells = scratch_cells;
 
-  // Buckets: longest work first within each, buckets in descending total work.
-  std::stable_sort(items.begin(), items.end(), [](const auto& a, const auto& b) {
-    if (!(a.first == b.first)) return a.first < b.first;
-    return a.second.work > b.second.work;
-  });
-  std::vector<uint32_t> order;
-  order.reserve(items.size());
-  P->buckets.clear();
-  std::vector<uint64_t> bwork;
-  for (size_t q = 0; q < items.size(); ++q) {
-    if (q == 0 || !(items[q].first == items[q - 1].first)) {
-      Bucket b;
-      b.kind = (PassKind)items[q].first.kind;
-      b.c = items[q].first.c;
-      b.wide = items[q].first.wide;
-      b.tb = items[q].first.tb;
-      b.lanes = items[q].first.lanes;
-      b.first = (uint32_t)order.size();
-      P->buckets.push_back(b);
-      bwork.push_back(0);
+  // Buckets in key order; within a bucket, longest work first (ties in job order).  The
+  // keys are few: a counting sort by bucket, then a sort by work inside each.
+  std::vector<Key2> keys2;
+  std::vector<uint32_t> kid(items.size());
+  {
+    int last = -1;
+    for (size_t q = 0; q < items.size(); ++q) {
+      const Key2& k = items[q].first;
+      if (last < 0 || !(keys2[last] == k)) {
+        last = -1;
+        for (size_t u = 0; u < keys2.size(); ++u)
+          if (keys2[u] == k) last = (int)u;
+        if (last < 0) {
+          keys2.push_back(k);
+          last = (int)keys2.size() - 1;
+        }
+      }
+      kid[q] = (uint32_t)last;
     }
-    order.push_back(items[q].second.slot);
-    P->buckets.back().count++;
-    bwork.back() += items[q].second.work;
+  }
+  std::vector<uint32_t> rank(keys2.size());
+  {
+    std::vector<uint32_t> idx(keys2.size());
+    for (size_t u = 0; u < idx.size(); ++u) idx[u] = (uint32_t)u;
+    std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return keys2[a] < keys2[b]; });
+    for (size_t u = 0; u < idx.size(); ++u) rank[idx[u]] = (uint32_t)u;
+  }
+  std::vector<uint64_t> start(keys2.size() + 1, 0), bwork(keys2.size(), 0);
+  for (size_t q = 0; q < items.size(); ++q) {
+    start[rank[kid[q]] + 1]++;
+    bwork[kid[q]] += items[q].second.work;
+  }
+  for (size_t u = 0; u < keys2.size(); ++u) start[u + 1] += start[u];
+  std::vector<std::pair<uint64_t, uint32_t>> byb(items.size());  // (work, job order) by bucket
+  {
+    std::vector<uint64_t> at(start.begin(), start.end() - 1);
+    for (size_t q = 0; q < items.size(); ++q) byb[at[rank[kid[q]]]++] = {items[q].second.work, (uint32_t)q};
+  }
+  std::vector<uint32_t> order(items.size());
+  P->buckets.clear();
+  std::vector<Key2> sorted_keys(keys2.size());
+  for (size_t u = 0; u < keys2.size(); ++u) sorted_keys[rank[u]] = keys2[u];
+  std::vector<uint64_t> bw(keys2.size());
+  for (size_t u = 0; u < keys2.size(); ++u) bw[rank[u]] = bwork[u];
+  bwork.swap(bw);
+  for (size_t u = 0; u < sorted_keys.size(); ++u) {
+    auto b0 = byb.begin() + (ptrdiff_t)start[u], b1 = byb.begin() + (ptrdiff_t)start[u + 1];
+    std::sort(b0, b1, [](const auto& a, const auto& b) {
+      return a.first != b.first ? a.first > b.first : a.second < b.second;
+    });
+    Bucket b;
+    b.kind = (PassKind)sorted_keys[u].kind;
+    b.c = sorted_keys[u].c;
+    b.wide = sorted_keys[u].wide;
+    b.tb = sorted_keys[u].tb;
+    b.lanes = sorted_keys[u].lanes;
+    b.first = (uint32_t)start[u];
+    b.count = (uint32_t)(start[u + 1] - start[u]);
+    P->buckets.push_back(b);
+    for (auto it = b0; it != b1; ++it) order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
   }
   // Launch shapes: persistent grids, at most what fits the device at once.  Wide buckets
   // may run concurrently (fan-out streams), so each gets its own scratch slice.
@@ -559,6 +604,8 @@ int plan_fetch(sf_plan* P) {
   if (P->n_my) CK(cudaMemcpyAsync(P->h_mout.p, P->d_mout.p, P->n_my * 4, cudaMemcpyDeviceToHost, ctx->s));
   if (P->n_walk) {
     CK(cudaMemcpyAsync(P->h_tres.p, P->d_tres.p, P->n_aff * sizeof(TRes), cudaMemcpyDeviceToHost, ctx->s));
+    if ((rc = P->h_total.ensure(64))) return rc;
+    CK(cudaMemcpyAsync(P->h_total.p, P->d_total.p, 8, cudaMemcpyDeviceToHost, ctx->s));
   }
   CK(cudaStreamSynchronize(ctx->s));
   return SF_OK;
@@ -777,12 +824,14 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
   return SF_OK;
 }
 
+// Fills `results` from the fetched per-pass records; with `copy_ops`, also copies the CIGARs
+// fetched into h_ops to `ops` (sf_plan_download copies them straight from the device).
 int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
-                 uint64_t total) {
+                 uint64_t total, bool copy_ops) {
   if (total && (!ops || ops_cap < total)) {
     return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
   }
-  if (total) std::memcpy(ops, P->h_ops.p, total * 4);
+  if (total && copy_ops) std::memcpy(ops, P->h_ops.p, total * 4);
   const DRes* rs = P->h_res.as<DRes>();
   const TRes* tr = P->h_tres.as<TRes>();
   const uint32_t* mo = P->h_mout.as<uint32_t>();
@@ -849,6 +898,7 @@ uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_byte
   // headroom on each.
   uint64_t b = pool_bytes + 256 * 4 + 4096;
   uint64_t scratch = 0;
+  const bool use16 = allow16();
   for (const Pass& p : passes) {
     b += (uint64_t)(p.m + p.n + 34) / 4 + 40 + 200;
     if (p.kind == PK_MYERS) continue;
@@ -858,7 +908,7 @@ uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_byte
     int c = 4;
     bool wide = false;
     PassKind kind = PK_AFFINE;
-    classify_affine(p, flags, wmax, kind, c, wide);
+    classify_affine(p, flags, wmax, use16, kind, c, wide);
     if (p.want_cigar && p.kind != PK_LOCAL) {
       b += (uint64_t)p.m * tb_row_words(c, wide ? wide_chunks(c, wmax) : 1) * 4;
       b += 2 * ((uint64_t)p.m + p.n + 2) * 4;
@@ -1244,10 +1294,15 @@ int sf_plan_download(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t o
   CK(cudaSetDevice(P->ctx->dev));
   int rc = plan_fetch(P);
   if (rc) return rc;
-  uint64_t total = 0;
-  if ((rc = plan_fetch_ops(P, total))) return rc;
+  // The CIGARs go from the device straight into the caller's buffer (a DMA when it is pinned).
+  const uint64_t total = P->n_walk ? *P->h_total.as<uint64_t>() : 0;
   if (ops_used) *ops_used = total;
-  return plan_results(P, results, ops, ops_cap, total);
+  if (total && (!ops || ops_cap < total)) return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
+  if (total) {
+    CK(cudaMemcpyAsync(ops, P->d_opsc.p, total * 4, cudaMemcpyDeviceToHost, P->ctx->s));
+    CK(cudaStreamSynchronize(P->ctx->s));
+  }
+  return plan_results(P, results, ops, ops_cap, total, false);
 }
 
 int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, const sf_job_t* jobs,
