@@ -373,6 +373,8 @@ def main():
     ap.add_argument("--plain-pairs", type=int, default=200)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cigar", type=int, default=1, help="c2/c3: traceback + CIGAR (1) or score only (0)")
+    ap.add_argument("--tune", type=int, default=None,
+                    help="autotune the length buckets' kernel classes first (default: c3 only)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -396,6 +398,17 @@ def main():
     ctx = B.Context(local)
     plan = B.Plan(ctx, jobs, pool.size)
     plan.upload(pool)
+    tune_report = None
+    if args.tune if args.tune is not None else args.config == "c3":
+        # Untimed: the autotuner picks each length bucket's kernel class (sf_plan_tune).
+        tune_report = plan.tune(pool, reps=2)
+    tune_map = {}
+    for g in (tune_report or {}).get("groups", []):
+        key = ("myers", g["c"], g["lanes"]) if g["kind"] == "myers" else \
+            (g["kind"], g["c"], bool(g["wide"]), bool(g["traceback"]))
+        ch = g["chosen"]
+        tune_map[key] = ("myers", ch["c"], ch["lanes"]) if g["kind"] == "myers" else \
+            (g["kind"], ch["c"], bool(g["wide"]), bool(g["traceback"]))
     stream = torch.cuda.ExternalStream(plan.stream(), device=local)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB
     for _ in range(args.warmup):
@@ -438,7 +451,7 @@ def main():
     avg = [statistics.mean(p[i] for p in prof) for i in range(len(prof[0]))]
     top = max(range(1, 1 + len(desc["buckets"])), key=lambda i: avg[i])
     tb = desc["buckets"][top - 1]
-    cls = job_classes(jobs, B)
+    cls = [tune_map.get(c, c) for c in job_classes(jobs, B)]
     key = ("myers", tb["c"], tb["lanes"]) if tb["kind"] == "myers" else \
         (tb["kind"], tb["c"], bool(tb["wide"]), bool(tb["traceback"]))
     sel = np.array([c == key for c in cls])
@@ -556,7 +569,18 @@ def main():
                            "pairs": int(len(jobs)),
                            "cells_per_step": cells, "l2": "flushed (256 MB write) before each step",
                            "parallelism": f"replicas x{ws}", "form": "batched persistent plan, CUDA graph",
-                           "buckets": len(desc["buckets"]), "status_nonzero": bad},
+                           "buckets": len(desc["buckets"]), "status_nonzero": bad,
+                           "autotune": None if tune_report is None else {
+                               "groups": len(tune_report["groups"]),
+                               "changed": sum(1 for g in tune_report["groups"]
+                                              if (g["chosen"]["c"], g["chosen"]["lanes"]) !=
+                                              (g["c"], g["lanes"])),
+                               "seconds": tune_report["seconds"],
+                               "choices": [f'{g["kind"]}-c{g["c"]}x{g["lanes"]}->'
+                                           f'c{g["chosen"]["c"]}x{g["chosen"]["lanes"]}'
+                                           for g in tune_report["groups"]
+                                           if (g["chosen"]["c"], g["chosen"]["lanes"]) !=
+                                           (g["c"], g["lanes"])]}},
                 "e2e": e2e, "plain": plain,
                 "batched_vs_plain": (value / plain["value"]) if plain else None,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,

@@ -267,6 +267,21 @@ const char *sf_plan_describe(sf_plan *plan);
 int sf_plan_profile(sf_plan *plan, float *ms, uint32_t cap,
                     uint32_t *n_stages);
 
+/* Autotuner (no reference counterpart: the reference's CPU path has no kernel
+ * classes to choose).  Groups the plan's jobs by their default kernel class
+ * (their length bucket) and times each group alone, `reps` executes per
+ * candidate, in the classes it may run in instead: Myers, every (blocks per
+ * lane, lanes per pair) that covers the group's longest pattern -- how much of
+ * a warp a pair takes; affine register rows, the next two row widths -- where
+ * the bucket edges fall.  The fastest per group is kept in the plan's context
+ * (later plans and sf_batch_run in that context use it) and the plan is rebuilt
+ * with it, its pool uploaded again from `pool`.  `report` (may be NULL)
+ * receives a JSON summary.  Results do not depend on the classes. */
+int sf_plan_tune(sf_plan *plan, const uint8_t *pool, uint32_t reps, char *report,
+                 uint64_t cap);
+/* Drops a context's autotuner choices: later plans use the default classes. */
+int sf_context_untune(sf_context *ctx);
+
 /* One call on the context's reusable plan: descriptors, upload, execute,
  * download (buffers grow and are reused across calls). */
 int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,

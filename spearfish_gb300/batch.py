@@ -49,6 +49,10 @@ class Context:
         _abi.check(self._lib.sf_context_create(int(device), C.byref(h)))
         self.handle = h
 
+    def untune(self) -> None:
+        """Drops the autotuner's choices: later plans use the default kernel classes."""
+        _abi.check(self._lib.sf_context_untune(self.handle))
+
     def close(self):
         if self.handle:
             self._lib.sf_context_destroy(self.handle)
@@ -117,6 +121,17 @@ class Plan:
 
     def describe(self) -> str:
         return self._lib.sf_plan_describe(self.handle).decode()
+
+    def tune(self, pool: np.ndarray, reps: int = 3) -> dict:
+        """Autotunes the kernel classes of this plan's length buckets (sf_plan_tune): the
+        choices stay in the context for later plans; the plan is rebuilt and its pool
+        uploaded again.  Returns the tuner's report."""
+        import json
+        pool = np.ascontiguousarray(pool, dtype=np.uint8)
+        buf = C.create_string_buffer(1 << 20)
+        _abi.check(self._lib.sf_plan_tune(self.handle, pool.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                          int(reps), buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def download(self, ops_cap: Optional[int] = None) -> Output:
         res = np.zeros(len(self.jobs), dtype=RESULT_DTYPE)

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <tuple>
 #include <memory>
 #include <string>
 #include <vector>
@@ -113,6 +115,24 @@ struct Pass {
   sf_affine_t sc{2, 4, 4, 2};
 };
 
+// A kernel class: what a pass runs on (kind, cells or blocks per lane, wide rows,
+// traceback, Myers lanes per pair).
+struct ClassKey {
+  int kind = 0, c = 0, wide = 0, tb = 0, lanes = 0;
+  bool operator<(const ClassKey& o) const {
+    return std::tie(kind, c, wide, tb, lanes) < std::tie(o.kind, o.c, o.wide, o.tb, o.lanes);
+  }
+  bool operator==(const ClassKey& o) const {
+    return kind == o.kind && c == o.c && wide == o.wide && tb == o.tb && lanes == o.lanes;
+  }
+};
+// The autotuner's choices (sf_plan_tune): default class of a pass -> the class it runs in
+// (affine: another C of the same kernel; Myers: blocks per lane and lanes per pair).
+struct ClassChoice {
+  int c = 0, lanes = 0;
+};
+using TuneTable = std::map<ClassKey, ClassChoice>;
+
 struct Bucket {
   PassKind kind;
   int c = 0;       // affine: cells per lane; Myers: blocks per lane
@@ -152,6 +172,8 @@ struct sf_plan {
   cudaGraphExec_t graph = nullptr;
   bool graph_tried = false;
   uint64_t launches = 0;
+  // Class overrides for this plan only (the autotuner's trial plans); else the context's.
+  const sfe::TuneTable* tune_override = nullptr;
   ~sf_plan() {
     if (graph) cudaGraphExecDestroy(graph);
     if (owns_ctx) delete ctx;
@@ -168,6 +190,7 @@ struct sf_context {
   cudaStream_t aux[kAux] = {};
   cudaEvent_t fork = nullptr, join[kAux] = {};
   std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
+  sfe::TuneTable tune;             // autotuner choices, applied to every later plan
   ~sf_context() {
     cache.reset();
     int prev = 0;

@@ -2,10 +2,12 @@
 // bucketing, HBM layout, persistent launches captured in a CUDA graph) and the one-call
 // entry points that mirror crates/map/src/align.rs.
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -105,6 +107,15 @@ void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, Pa
   }
   kind = p.kind == PK_LOCAL ? PK_LOCAL : PK_AFFINE;
   choose_affine_class(wmax, c, wide);
+}
+
+// The autotuner's override for a pass's default class, if it chose one.
+void apply_tune(const TuneTable* tune, int kind, int& c, bool wide, bool tb, int& lanes) {
+  if (!tune || tune->empty()) return;
+  auto it = tune->find(ClassKey{kind, c, wide ? 1 : 0, tb ? 1 : 0, lanes});
+  if (it == tune->end()) return;
+  c = it->second.c;
+  lanes = it->second.lanes;
 }
 
 int choose_myers_class(uint32_t m, int& b, int& lanes) {
@@ -220,6 +231,7 @@ int plan_build(sf_plan* P) {
   std::vector<std::pair<Key2, Item>> items;
   items.reserve(np);
   const bool use16 = allow16();
+  const TuneTable* tune = P->tune_override ? P->tune_override : &ctx->tune;
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
@@ -227,6 +239,7 @@ int plan_build(sf_plan* P) {
       int b = 1, lanes = 1;
       int rc = choose_myers_class(p.m, b, lanes);
       if (rc) return rc;
+      apply_tune(tune, PK_MYERS, b, false, false, lanes);
       MJob m{};
       m.p_word = word_of[2 * q];
       m.t_word = word_of[2 * q + 1];
@@ -250,6 +263,10 @@ int plan_build(sf_plan* P) {
     PassKind kind = PK_AFFINE;
     classify_affine(p, flags, wmax, use16, kind, c, wide);
     const bool tb = p.want_cigar && p.kind != PK_LOCAL;
+    if (!wide) {
+      int ln = 32;
+      apply_tune(tune, kind, c, false, tb, ln);
+    }
     if (tb) {
       flags |= F_TB;
       j.tb_word = tb_words;
@@ -1323,6 +1340,164 @@ int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, cons
   if ((rc = plan_upload_from(P, pool))) return rc;
   if ((rc = plan_execute(P, false))) return rc;
   return sf_plan_download(P, results, ops, ops_cap, ops_used);
+}
+
+namespace {
+
+// A pass's class before any override, and the Myers blocks it needs.
+int default_class(const Pass& p, bool use16, ClassKey& key, int64_t& blocks) {
+  if (p.kind == PK_MYERS) {
+    int b = 1, lanes = 1;
+    int rc = choose_myers_class(p.m, b, lanes);
+    if (rc) return rc;
+    key = ClassKey{PK_MYERS, b, 0, 0, lanes};
+    blocks = ((int64_t)p.m + 63) / 64;
+    return SF_OK;
+  }
+  uint32_t flags = 0;
+  DJob j = make_djob(p, flags);
+  const int64_t wmax = band_wmax(j, flags);
+  int c = 4;
+  bool wide = false;
+  PassKind kind = PK_AFFINE;
+  classify_affine(p, flags, wmax, use16, kind, c, wide);
+  const bool tb = p.want_cigar && p.kind != PK_LOCAL;
+  key = ClassKey{kind, c, wide ? 1 : 0, tb ? 1 : 0, 32};
+  blocks = 0;
+  return SF_OK;
+}
+
+// The classes a group of passes may run in instead of its default: Myers, every
+// (blocks per lane, lanes per pair) that covers the group's longest pattern; affine
+// register rows, the default C and the next two classes of the same kernel.
+std::vector<ClassChoice> tune_candidates(const ClassKey& key, int64_t blocks) {
+  std::vector<ClassChoice> out;
+  out.push_back(ClassChoice{key.c, key.lanes});
+  if (key.kind == PK_MYERS) {
+    for (int q = 0; q < sfk::kMyersNB; ++q) {
+      const int b = sfk::kMyersB[q];
+      int lanes = 1;
+      while ((int64_t)lanes * b < blocks) lanes <<= 1;
+      if (lanes > 32) continue;
+      bool dup = false;
+      for (const auto& c : out) dup = dup || (c.c == b && c.lanes == lanes);
+      if (!dup) out.push_back(ClassChoice{b, lanes});
+    }
+  } else if (!key.wide) {
+    const int* cs = key.kind == PK_AFFINE16 ? sfk::kAffine16C : sfk::kAffineC;
+    const int nc = key.kind == PK_AFFINE16 ? sfk::kAffine16NC : sfk::kAffineNC;
+    for (int q = 0; q < nc; ++q)
+      if (cs[q] > key.c && (int)out.size() < 3) out.push_back(ClassChoice{cs[q], 32});
+  }
+  return out;
+}
+
+}  // namespace
+
+int sf_plan_tune(sf_plan* P, const uint8_t* pool, uint32_t reps, char* report, uint64_t cap) {
+  if (!P || (P->pool_bytes && !pool)) return fail(SF_ERR_INVALID, "bad argument");
+  sf_context* ctx = P->ctx;
+  CK(cudaSetDevice(ctx->dev));
+  if (reps == 0) reps = 1;
+  const auto t0 = std::chrono::steady_clock::now();
+  const bool use16 = allow16();
+  // Group the passes by their default class.
+  std::map<ClassKey, std::vector<size_t>> groups;
+  std::map<ClassKey, int64_t> gblocks;
+  for (size_t q = 0; q < P->passes.size(); ++q) {
+    ClassKey k;
+    int64_t blocks = 0;
+    int rc = default_class(P->passes[q], use16, k, blocks);
+    if (rc) return rc;
+    groups[k].push_back(q);
+    gblocks[k] = std::max(gblocks[k], blocks);
+  }
+  sf_plan S;  // trial plan, its buffers reused across trials
+  S.ctx = ctx;
+  S.pool_bytes = P->pool_bytes;
+  void* uploaded = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  std::string rep = "{\"groups\": [";
+  int rc = SF_OK;
+  size_t gi = 0;
+  for (auto& g : groups) {
+    const ClassKey& key = g.first;
+    const std::vector<ClassChoice> cands = tune_candidates(key, gblocks[key]);
+    S.passes.clear();
+    for (size_t q : g.second) S.passes.push_back(P->passes[q]);
+    float best_ms = -1;
+    ClassChoice best = cands[0];
+    std::string tried;
+    for (size_t ci = 0; ci < cands.size() && rc == SF_OK; ++ci) {
+      TuneTable t1;
+      t1[key] = cands[ci];
+      S.tune_override = &t1;
+      if ((rc = plan_build(&S))) break;
+      if (S.d_bytes.p != uploaded) {
+        if ((rc = plan_upload_from(&S, pool))) break;
+        uploaded = S.d_bytes.p;
+      }
+      if ((rc = plan_launch(&S, ctx->s))) break;  // warm-up
+      CK(cudaEventRecord(e0, ctx->s));
+      for (uint32_t r = 0; r < reps && rc == SF_OK; ++r) rc = plan_launch(&S, ctx->s);
+      CK(cudaEventRecord(e1, ctx->s));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      ms /= (float)reps;
+      char buf[96];
+      std::snprintf(buf, sizeof buf, "%s{\"c\": %d, \"lanes\": %d, \"ms\": %.4f}", ci ? ", " : "",
+                    cands[ci].c, cands[ci].lanes, ms);
+      tried += buf;
+      if (best_ms < 0 || ms < best_ms) {
+        best_ms = ms;
+        best = cands[ci];
+      }
+    }
+    S.tune_override = nullptr;
+    if (rc) break;
+    if (best.c == key.c && best.lanes == key.lanes)
+      ctx->tune.erase(key);
+    else
+      ctx->tune[key] = best;
+    char buf[256];
+    std::snprintf(buf, sizeof buf,
+                  "%s{\"kind\": \"%s\", \"c\": %d, \"wide\": %s, \"traceback\": %s, \"lanes\": %d, "
+                  "\"jobs\": %zu, \"chosen\": {\"c\": %d, \"lanes\": %d}, \"tried\": [",
+                  gi++ ? ", " : "",
+                  key.kind == PK_MYERS ? "myers"
+                                       : (key.kind == PK_LOCAL ? "local"
+                                                               : (key.kind == PK_AFFINE16 ? "affine16" : "affine")),
+                  key.c, key.wide ? "true" : "false", key.tb ? "true" : "false", key.lanes,
+                  g.second.size(), best.c, best.lanes);
+    rep += buf + tried + "]}";
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  // The plan itself now runs with the chosen classes.
+  if ((rc = plan_build(P))) return rc;
+  if ((rc = plan_upload_from(P, pool))) return rc;
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  char tail[64];
+  std::snprintf(tail, sizeof tail, "], \"seconds\": %.3f}", secs);
+  rep += tail;
+  if (report && cap) {
+    const size_t n = std::min<size_t>(rep.size(), cap - 1);
+    std::memcpy(report, rep.data(), n);
+    report[n] = 0;
+    if (rep.size() >= cap) return fail(SF_ERR_CAPACITY, "report longer than its buffer");
+  }
+  return SF_OK;
+}
+
+int sf_context_untune(sf_context* ctx) {
+  if (!ctx) return fail(SF_ERR_INVALID, "null context");
+  ctx->tune.clear();
+  return SF_OK;
 }
 
 int sf_plan_profile(sf_plan* P, float* ms, uint32_t cap, uint32_t* n_stages) {
