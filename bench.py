@@ -374,7 +374,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cigar", type=int, default=1, help="c2/c3: traceback + CIGAR (1) or score only (0)")
     ap.add_argument("--tune", type=int, default=None,
-                    help="autotune the length buckets' kernel classes first (default: c3 only)")
+                    help="autotune the length buckets' kernel classes first (default: on)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -399,7 +399,7 @@ def main():
     plan = B.Plan(ctx, jobs, pool.size)
     plan.upload(pool)
     tune_report = None
-    if args.tune if args.tune is not None else args.config == "c3":
+    if args.tune is None or args.tune:
         # Untimed: the autotuner picks each length bucket's kernel class (sf_plan_tune).
         tune_report = plan.tune(pool, reps=2)
     tune_map = {}
