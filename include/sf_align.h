@@ -290,6 +290,43 @@ int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                  sf_result_t *results, uint32_t *ops, uint64_t ops_cap,
                  uint64_t *ops_used);
 
+/* ---- tie-break batching (map/src/lib.rs) --------------------------------
+ * The mapper's tie-break asks, per read, for the edit distance to each of its
+ * candidate texts under a threshold that tightens as it goes
+ * (lib.rs:851-911 `Mapper::banded`).  Here a whole read batch's distinct
+ * (read, text) distances run as one Myers launch, and each read's threshold is
+ * applied in text order on the host -- the same values, since a batch
+ * distance is exact whenever it is within its threshold (align.rs:87-168). */
+
+/* lib.rs:851-911 `Mapper::banded`: out[q] = the distance of `read` to
+ * texts[q] in `mode`, or k + 1 when it exceeds k = (best so far + cap)
+ * (saturating); with distinct = 0 a repeated text is computed once and its
+ * first value re-capped at the current k. */
+int sf_banded(const uint8_t *read, uint64_t m, const uint8_t *const *texts,
+              const uint64_t *lens, uint64_t count, int mode, uint32_t cap,
+              int distinct, uint32_t *out);
+
+typedef struct {
+    uint64_t off, len; /* codes in the pool */
+} sf_span_t;
+
+typedef struct {
+    uint64_t p_off;    /* the read's codes in the pool */
+    uint64_t first;    /* index of its first text in the text list */
+    uint32_t m;        /* read length */
+    uint32_t count;    /* its texts: text list [first, first + count) */
+    uint32_t mode;     /* sf_mode */
+    uint32_t cap;      /* `banded`'s cap */
+    uint32_t distinct; /* `banded`'s distinct */
+    uint32_t pad_;
+} sf_banded_read_t;
+
+/* `banded` for n_reads reads at once (their texts consecutive in `texts`):
+ * out[q] for texts[q], as sf_banded would give read by read. */
+int sf_banded_batch(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
+                    const sf_banded_read_t *reads, uint64_t n_reads,
+                    const sf_span_t *texts, uint64_t n_texts, uint32_t *out);
+
 /* ---- serving: continuous batching ---------------------------------------
  * Requests (the jobs of a read batch over a byte pool the caller keeps alive
  * until it waits for them) are admitted in arrival order as soon as a slot

@@ -52,6 +52,16 @@ class JobT(C.Structure):
                 ("xdrop", C.c_int32), ("sc_index", C.c_uint32)]
 
 
+class SpanT(C.Structure):
+    _fields_ = [("off", C.c_uint64), ("len", C.c_uint64)]
+
+
+class BandedReadT(C.Structure):
+    _fields_ = [("p_off", C.c_uint64), ("first", C.c_uint64), ("m", C.c_uint32),
+                ("count", C.c_uint32), ("mode", C.c_uint32), ("cap", C.c_uint32),
+                ("distinct", C.c_uint32), ("pad_", C.c_uint32)]
+
+
 class ResultT(C.Structure):
     _fields_ = [("score", C.c_int32), ("distance", C.c_uint32), ("pattern_end", C.c_uint64),
                 ("text_start", C.c_uint64), ("text_end", C.c_uint64), ("text_read", C.c_uint64),
@@ -92,6 +102,10 @@ SIGNATURES = {
     "sf_distance": (C.c_int, [_u8p, C.c_uint64, _u8p, C.c_uint64, C.c_int, C.c_uint32, _u32p]),
     "sf_batch_distances": (C.c_int, [_u8p, C.c_uint64, _u8pp, _u64p, C.c_uint64, C.c_int,
                                      C.c_uint32, _u32p]),
+    "sf_banded": (C.c_int, [_u8p, C.c_uint64, _u8pp, _u64p, C.c_uint64, C.c_int, C.c_uint32,
+                            C.c_int, _u32p]),
+    "sf_banded_batch": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(BandedReadT), C.c_uint64,
+                                  C.POINTER(SpanT), C.c_uint64, _u32p]),
     "sf_infix_distance": (C.c_int, [_u8p, C.c_uint64, _u8p, C.c_uint64, _u32p]),
     "sf_affine": (C.c_int, [_u8p, C.c_uint64, _u8p, C.c_uint64, C.c_int, _aff, C.c_uint64,
                             _i32p]),

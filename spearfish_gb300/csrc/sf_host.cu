@@ -12,6 +12,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "sf_engine.h"
@@ -1320,6 +1321,179 @@ int sf_plan_download(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t o
     CK(cudaStreamSynchronize(P->ctx->s));
   }
   return plan_results(P, results, ops, ops_cap, total, false);
+}
+
+// ---- tie-break batching (map/src/lib.rs:851-911 `Mapper::banded`) ------------------------
+
+namespace {
+
+uint32_t sat_add_u32(uint32_t a, uint32_t b) { return a > UINT32_MAX - b ? UINT32_MAX : a + b; }
+
+// A read's texts: which are first occurrences, and each repeat's first occurrence.  The
+// reference keys texts by their bytes (lib.rs:858-877); here by an FNV-1a hash, equal
+// hashes compared byte by byte.
+void dedup_texts(const uint8_t* const* tx, const uint64_t* len, uint64_t count, bool distinct,
+                 std::vector<uint32_t>& first_of, std::vector<uint8_t>& is_first) {
+  first_of.resize(count);
+  is_first.resize(count);
+  if (distinct) {
+    for (uint64_t q = 0; q < count; ++q) {
+      first_of[q] = (uint32_t)q;
+      is_first[q] = 1;
+    }
+    return;
+  }
+  std::unordered_map<uint64_t, std::vector<uint32_t>> seen;
+  for (uint64_t q = 0; q < count; ++q) {
+    uint64_t h = 1469598103934665603ull ^ len[q];
+    for (uint64_t i = 0; i < len[q]; ++i) {
+      h ^= tx[q][i];
+      h *= 1099511628211ull;
+    }
+    auto& v = seen[h];
+    int64_t hit = -1;
+    for (uint32_t u : v)
+      if (len[u] == len[q] && (len[q] == 0 || std::memcmp(tx[u], tx[q], len[q]) == 0)) {
+        hit = u;
+        break;
+      }
+    if (hit < 0) {
+      v.push_back((uint32_t)q);
+      first_of[q] = (uint32_t)q;
+      is_first[q] = 1;
+    } else {
+      first_of[q] = (uint32_t)hit;
+      is_first[q] = 0;
+    }
+  }
+}
+
+// lib.rs:880-909: in text order, k = best so far + cap; a first occurrence's distance is
+// exact when <= k, else k + 1 (the batch kernel's distances are exact, so the threshold is
+// applied here); a repeat takes its first occurrence's value re-capped at the current k.
+void banded_finish(uint64_t count, const std::vector<uint32_t>& first_of,
+                   const std::vector<uint8_t>& is_first, const uint32_t* dist, uint32_t cap,
+                   uint32_t* out) {
+  std::vector<uint32_t> val(count, 0);
+  uint32_t best = UINT32_MAX;
+  for (uint64_t q = 0; q < count; ++q) {
+    const uint32_t k = sat_add_u32(best, cap);
+    if (!is_first[q]) {
+      const uint32_t d = val[first_of[q]];
+      out[q] = d <= k ? d : sat_add_u32(k, 1);
+      continue;
+    }
+    const uint32_t d = dist[q] <= k ? dist[q] : sat_add_u32(k, 1);
+    best = std::min(best, d);
+    val[q] = d;
+    out[q] = d;
+  }
+}
+
+}  // namespace
+
+int sf_banded(const uint8_t* read, uint64_t m, const uint8_t* const* texts, const uint64_t* lens,
+              uint64_t count, int mode, uint32_t cap, int distinct, uint32_t* out) {
+  if (!ok_mode(mode) || (count && (!texts || !lens || !out)) || (m && !read))
+    return fail(SF_ERR_INVALID, "bad argument");
+  if (!count) return SF_OK;
+  for (uint64_t q = 0; q < count; ++q)
+    if (lens[q] && !texts[q]) return fail(SF_ERR_INVALID, "null text");
+  std::vector<uint32_t> first_of;
+  std::vector<uint8_t> is_first;
+  dedup_texts(texts, lens, count, distinct != 0, first_of, is_first);
+  Gather g;
+  const uint64_t po = g.add(read, m);
+  std::vector<Pass> ps;
+  std::vector<uint64_t> text_of;
+  for (uint64_t q = 0; q < count; ++q) {
+    if (!is_first[q]) continue;
+    Pass p;
+    p.kind = PK_MYERS;
+    p.mode = (uint8_t)mode;
+    p.k = SF_NONE;
+    p.p_off = po;
+    p.m = (uint32_t)m;
+    p.t_off = g.add(texts[q], lens[q]);
+    p.n = (uint32_t)lens[q];
+    ps.push_back(p);
+    text_of.push_back(q);
+  }
+  std::vector<uint32_t> mo;
+  int rc = run_passes(ps, g, nullptr, &mo, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  std::vector<uint32_t> dist(count, 0);
+  for (size_t u = 0; u < text_of.size(); ++u) dist[text_of[u]] = mo[u];
+  banded_finish(count, first_of, is_first, dist.data(), cap, out);
+  return SF_OK;
+}
+
+int sf_banded_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
+                    const sf_banded_read_t* reads, uint64_t n_reads, const sf_span_t* texts,
+                    uint64_t n_texts, uint32_t* out) {
+  if (!ctx || (n_reads && !reads) || (n_texts && (!texts || !out)) || (pool_bytes && !pool))
+    return fail(SF_ERR_INVALID, "bad argument");
+  // Per read: its distinct texts become Myers jobs of the one batch.
+  std::vector<std::vector<uint32_t>> first_of(n_reads);
+  std::vector<std::vector<uint8_t>> is_first(n_reads);
+  std::vector<sf_job_t> jobs;
+  std::vector<uint64_t> job_text;  // the text index of each job
+  std::vector<const uint8_t*> tp;
+  std::vector<uint64_t> tl;
+  for (uint64_t r = 0; r < n_reads; ++r) {
+    const sf_banded_read_t& R = reads[r];
+    if (!ok_mode((int)R.mode)) return fail(SF_ERR_INVALID, "bad mode");
+    if (R.first > n_texts || R.count > n_texts - R.first)
+      return fail(SF_ERR_INVALID, "read's texts outside the text list");
+    if (R.p_off > pool_bytes || R.m > pool_bytes - R.p_off)
+      return fail(SF_ERR_INVALID, "read outside the pool");
+    tp.resize(R.count);
+    tl.resize(R.count);
+    for (uint64_t q = 0; q < R.count; ++q) {
+      const sf_span_t& t = texts[R.first + q];
+      if (t.off > pool_bytes || t.len > pool_bytes - t.off)
+        return fail(SF_ERR_INVALID, "text outside the pool");
+      tp[q] = pool + t.off;
+      tl[q] = t.len;
+    }
+    dedup_texts(tp.data(), tl.data(), R.count, R.distinct != 0, first_of[r], is_first[r]);
+    for (uint64_t q = 0; q < R.count; ++q) {
+      if (!is_first[r][q]) continue;
+      sf_job_t j{};
+      j.kind = SF_JOB_MYERS;
+      j.mode = (uint8_t)R.mode;
+      j.k = SF_NONE;
+      j.band = SF_NOLIMIT;
+      j.p_off = R.p_off;
+      j.m = R.m;
+      j.t_off = texts[R.first + q].off;
+      j.n = (uint32_t)texts[R.first + q].len;
+      if (texts[R.first + q].len >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+      jobs.push_back(j);
+      job_text.push_back(R.first + q);
+    }
+  }
+  std::vector<uint32_t> dist(n_texts, 0);
+  if (!jobs.empty()) {
+    if (!ctx->cache) {
+      ctx->cache.reset(new sf_plan);
+      ctx->cache->ctx = ctx;
+    }
+    sf_plan* P = ctx->cache.get();
+    int rc = jobs_to_passes(jobs.data(), jobs.size(), nullptr, 0, pool_bytes, P->passes);
+    if (rc) return rc;
+    P->pool_bytes = pool_bytes;
+    if ((rc = plan_build(P))) return rc;
+    if ((rc = plan_upload_from(P, pool))) return rc;
+    if ((rc = plan_execute(P, false))) return rc;
+    if ((rc = plan_fetch(P))) return rc;
+    const uint32_t* mo = P->h_mout.as<uint32_t>();
+    for (size_t u = 0; u < jobs.size(); ++u) dist[job_text[u]] = mo[P->slot[u]];
+  }
+  for (uint64_t r = 0; r < n_reads; ++r)
+    banded_finish(reads[r].count, first_of[r], is_first[r], dist.data() + reads[r].first,
+                  reads[r].cap, out + reads[r].first);
+  return SF_OK;
 }
 
 int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, const sf_job_t* jobs,

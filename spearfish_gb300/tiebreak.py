@@ -1,0 +1,62 @@
+"""Tie-break batching: the mapper's per-read distance calls (map/src/lib.rs:851-911
+`Mapper::banded`) for one read, or for a whole read batch in one device launch
+(include/sf_align.h, "tie-break batching").
+
+``banded(read, texts, mode, cap, distinct)`` returns, per text in order, the edit distance
+or k + 1 when it exceeds k = (best so far + cap), as the reference does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _abi
+from .align import _codes, _ptr, _Texts
+from .batch import Context, PoolBuilder
+
+NONE = 0xFFFFFFFF
+
+
+def banded(read, texts: Sequence, mode: int, cap: int, distinct: bool = False) -> list[int]:
+    """lib.rs:851-911 `Mapper::banded` (one read; the one-call context)."""
+    if not texts:
+        return []
+    r = _codes(read)
+    tx = _Texts(texts)
+    out = np.zeros(len(texts), dtype=np.uint32)
+    _abi.check(_abi.load().sf_banded(_ptr(r), r.size, *tx.args(), int(mode), int(cap),
+                                     int(bool(distinct)),
+                                     out.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return [int(v) for v in out]
+
+
+def banded_batch(ctx: Context, reads: Sequence) -> list[list[int]]:
+    """`banded` for many reads in one device batch: reads = [(read, texts, mode, cap,
+    distinct), ...]; returns each read's list."""
+    pb = PoolBuilder()
+    rs = (_abi.BandedReadT * max(1, len(reads)))()
+    spans = []
+    for i, (read, texts, mode, cap, distinct) in enumerate(reads):
+        r = rs[i]
+        r.p_off = pb.add(read)
+        r.m = len(read)
+        r.first = len(spans)
+        r.count = len(texts)
+        r.mode = int(mode)
+        r.cap = int(cap)
+        r.distinct = int(bool(distinct))
+        for t in texts:
+            spans.append((pb.add(t), len(t)))
+    pool = pb.build()
+    sp = (_abi.SpanT * max(1, len(spans)))(*[_abi.SpanT(o, n) for o, n in spans])
+    out = np.zeros(max(1, len(spans)), dtype=np.uint32)
+    _abi.check(_abi.load().sf_banded_batch(
+        ctx.handle, pool.ctypes.data_as(C.POINTER(C.c_uint8)), pool.size, rs, len(reads), sp,
+        len(spans), out.ctypes.data_as(C.POINTER(C.c_uint32))))
+    res, at = [], 0
+    for _, texts, *_ in reads:
+        res.append([int(v) for v in out[at:at + len(texts)]])
+        at += len(texts)
+    return res

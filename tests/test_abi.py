@@ -42,6 +42,8 @@ def test_struct_layouts(lib):
     assert C.sizeof(_abi.ExtendT) == 32
     assert C.sizeof(_abi.CutT) == 16
     assert C.sizeof(_abi.CigarT) == 40
+    assert C.sizeof(_abi.SpanT) == 16
+    assert C.sizeof(_abi.BandedReadT) == 40
     assert batch.JOB_DTYPE.itemsize == 80 and batch.RESULT_DTYPE.itemsize == 64
 
 
