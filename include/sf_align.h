@@ -213,7 +213,9 @@ typedef struct {
     uint8_t kind;   /* SF_JOB_* */
     uint8_t mode;   /* sf_mode (Myers, affine) */
     uint8_t want_cigar;
-    uint8_t pad_;
+    uint8_t text_src; /* SF_TEXT_POOL: t_off is a byte offset in the pool;
+                         SF_TEXT_STORE: t_off is a base position in the context's
+                         transcript store (sf_context_use_store) */
     uint32_t k;      /* Myers threshold (SF_NONE: none) */
     uint64_t band;   /* affine band (SF_NOLIMIT: none) */
     uint64_t window; /* extend window */
@@ -289,6 +291,31 @@ int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                  const sf_affine_t *scores, uint32_t n_scores,
                  sf_result_t *results, uint32_t *ops, uint64_t ops_cap,
                  uint64_t *ops_used);
+
+/* ---- device-resident transcript store ------------------------------------
+ * The index's transcripts packed once in HBM, 2 bits a base in its own bit
+ * order (crates/index/src/lib.rs:47-153 `tx_seq`, 253-280: 32 bases per u64,
+ * base p at bits 2*(p % 32) of word p / 32).  Jobs of a plan built in a context
+ * that uses the store (sf_context_use_store) may name their text as a window
+ * of it (text_src = SF_TEXT_STORE, t_off = the window's first base in the
+ * store's concatenation, as `tx_range` numbers it; n = its length): the window
+ * is sliced on the device, so a batch uploads only reads and descriptors.  The
+ * store must outlive every plan execution that reads it. */
+enum { SF_TEXT_POOL = 0, SF_TEXT_STORE = 1 };
+typedef struct sf_store sf_store;
+
+/* A store of `count` transcripts given as byte codes (0..3), concatenated in
+ * `codes`, lens[q] codes each, on the context's device. */
+int sf_store_create(sf_context *ctx, const uint8_t *codes, const uint64_t *lens,
+                    uint64_t count, sf_store **out);
+/* A store from the index's packed words as they are (`tx_seq`, `bases` bases). */
+int sf_store_create_packed(sf_context *ctx, const uint64_t *tx_seq, uint64_t bases,
+                           sf_store **out);
+void sf_store_destroy(sf_store *store);
+/* Bases the store holds. */
+uint64_t sf_store_bases(const sf_store *store);
+/* Later plans of this context resolve SF_TEXT_STORE texts in `store` (NULL: none). */
+int sf_context_use_store(sf_context *ctx, sf_store *store);
 
 /* ---- tie-break batching (map/src/lib.rs) --------------------------------
  * The mapper's tie-break asks, per read, for the edit distance to each of its

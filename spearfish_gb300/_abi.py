@@ -46,7 +46,7 @@ class CigarT(C.Structure):
 class JobT(C.Structure):
     _fields_ = [("p_off", C.c_uint64), ("t_off", C.c_uint64), ("m", C.c_uint32),
                 ("n", C.c_uint32), ("kind", C.c_uint8), ("mode", C.c_uint8),
-                ("want_cigar", C.c_uint8), ("pad_", C.c_uint8), ("k", C.c_uint32),
+                ("want_cigar", C.c_uint8), ("text_src", C.c_uint8), ("k", C.c_uint32),
                 ("band", C.c_uint64), ("window", C.c_uint64), ("dlo", C.c_int64),
                 ("dhi", C.c_int64), ("end_bonus", C.c_int32), ("end_bonus2", C.c_int32),
                 ("xdrop", C.c_int32), ("sc_index", C.c_uint32)]
@@ -102,6 +102,11 @@ SIGNATURES = {
     "sf_distance": (C.c_int, [_u8p, C.c_uint64, _u8p, C.c_uint64, C.c_int, C.c_uint32, _u32p]),
     "sf_batch_distances": (C.c_int, [_u8p, C.c_uint64, _u8pp, _u64p, C.c_uint64, C.c_int,
                                      C.c_uint32, _u32p]),
+    "sf_store_create": (C.c_int, [_vp, _u8p, _u64p, C.c_uint64, C.POINTER(_vp)]),
+    "sf_store_create_packed": (C.c_int, [_vp, _u64p, C.c_uint64, C.POINTER(_vp)]),
+    "sf_store_destroy": (None, [_vp]),
+    "sf_store_bases": (C.c_uint64, [_vp]),
+    "sf_context_use_store": (C.c_int, [_vp, _vp]),
     "sf_banded": (C.c_int, [_u8p, C.c_uint64, _u8pp, _u64p, C.c_uint64, C.c_int, C.c_uint32,
                             C.c_int, _u32p]),
     "sf_banded_batch": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(BandedReadT), C.c_uint64,

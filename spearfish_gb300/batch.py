@@ -20,7 +20,7 @@ from .align import Affine, Mode, _aff
 JOB_MYERS, JOB_AFFINE, JOB_EXTEND_WINDOW, JOB_LOCAL = 0, 1, 2, 3
 
 JOB_DTYPE = np.dtype([("p_off", "<u8"), ("t_off", "<u8"), ("m", "<u4"), ("n", "<u4"),
-                      ("kind", "u1"), ("mode", "u1"), ("want_cigar", "u1"), ("pad_", "u1"),
+                      ("kind", "u1"), ("mode", "u1"), ("want_cigar", "u1"), ("text_src", "u1"),
                       ("k", "<u4"), ("band", "<u8"), ("window", "<u8"), ("dlo", "<i8"),
                       ("dhi", "<i8"), ("end_bonus", "<i4"), ("end_bonus2", "<i4"),
                       ("xdrop", "<i4"), ("sc_index", "<u4")], align=True)
@@ -49,6 +49,10 @@ class Context:
         _abi.check(self._lib.sf_context_create(int(device), C.byref(h)))
         self.handle = h
 
+    def use_store(self, store: Optional["Store"]) -> None:
+        """Later plans resolve TEXT_STORE texts in `store` (None: no store)."""
+        _abi.check(self._lib.sf_context_use_store(self.handle, store.handle if store else None))
+
     def untune(self) -> None:
         """Drops the autotuner's choices: later plans use the default kernel classes."""
         _abi.check(self._lib.sf_context_untune(self.handle))
@@ -59,6 +63,49 @@ class Context:
             self.handle = None
 
     def __del__(self):  # pragma: no cover - interpreter teardown
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+TEXT_POOL, TEXT_STORE = 0, 1
+
+
+class Store:
+    """The index's transcripts packed once in HBM (sf_store_*): jobs of plans built in a
+    context that uses it name texts as windows (text_src = TEXT_STORE, t_off = the first
+    base in the transcripts' concatenation, n = the window's length)."""
+
+    def __init__(self, ctx: "Context", transcripts=None, packed=None, bases: int = 0):
+        self._lib = _abi.load()
+        h = C.c_void_p()
+        if packed is not None:
+            w = np.ascontiguousarray(packed, dtype=np.uint64)
+            _abi.check(self._lib.sf_store_create_packed(
+                ctx.handle, w.ctypes.data_as(C.POINTER(C.c_uint64)), int(bases), C.byref(h)))
+            self.starts = None
+        else:
+            parts = [np.ascontiguousarray(np.asarray(t, dtype=np.uint8)) for t in transcripts]
+            lens = np.array([p.size for p in parts], dtype=np.uint64)
+            codes = np.concatenate(parts) if parts else np.zeros(1, np.uint8)
+            _abi.check(self._lib.sf_store_create(
+                ctx.handle, codes.ctypes.data_as(C.POINTER(C.c_uint8)),
+                lens.ctypes.data_as(C.POINTER(C.c_uint64)), len(parts), C.byref(h)))
+            self.starts = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.uint64) \
+                if len(parts) else np.zeros(0, np.uint64)
+        self.handle = h
+
+    @property
+    def bases(self) -> int:
+        return int(self._lib.sf_store_bases(self.handle))
+
+    def close(self):
+        if self.handle:
+            self._lib.sf_store_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
         try:
             self.close()
         except Exception:

@@ -145,6 +145,8 @@ struct Bucket {
 
 }  // namespace sfe
 
+struct sf_store;
+
 struct sf_plan {
   using Pass = sfe::Pass;
   using Bucket = sfe::Bucket;
@@ -172,6 +174,8 @@ struct sf_plan {
   cudaGraphExec_t graph = nullptr;
   bool graph_tried = false;
   uint64_t launches = 0;
+  // The transcript store SF_TEXT_STORE texts were resolved in (the context's at build time).
+  const sf_store* store = nullptr;
   // Class overrides for this plan only (the autotuner's trial plans); else the context's.
   const sfe::TuneTable* tune_override = nullptr;
   ~sf_plan() {
@@ -182,6 +186,17 @@ struct sf_plan {
 
 // ---- context ---------------------------------------------------------------------------
 
+// The transcript store: packed words, base p of the index's concatenation at position
+// p + kStorePad (one leading word of padding, so that every window has a base before it).
+struct sf_store {
+  int dev = 0;
+  uint64_t bases = 0;
+  sfe::DevBuf words;
+};
+constexpr uint64_t kStorePad = 16;
+// Pass::t_off of a store window: the flag plus the window's first position in the store.
+constexpr uint64_t kStoreFlag = uint64_t(1) << 63;
+
 struct sf_context {
   int dev = 0;
   int sms = 0;
@@ -191,6 +206,7 @@ struct sf_context {
   cudaEvent_t fork = nullptr, join[kAux] = {};
   std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
   sfe::TuneTable tune;             // autotuner choices, applied to every later plan
+  sf_store* store = nullptr;       // transcript store for SF_TEXT_STORE texts
   ~sf_context() {
     cache.reset();
     int prev = 0;
@@ -211,7 +227,8 @@ namespace sfe {
 
 int make_context(int device, sf_context** out);
 int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
-                   uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps);
+                   uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps,
+                   const sf_store* store = nullptr);
 // Descriptors, buckets and device buffers for P->passes (pool not yet uploaded).
 int plan_build(sf_plan* P);
 int plan_upload_from(sf_plan* P, const uint8_t* pool);

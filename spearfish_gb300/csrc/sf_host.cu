@@ -180,8 +180,11 @@ int plan_build(sf_plan* P) {
   keys.reserve(2 * np);
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
-    if (p.p_off + p.m > P->pool_bytes || p.t_off + p.n > P->pool_bytes)
+    if (p.p_off + p.m > P->pool_bytes ||
+        (!(p.t_off & kStoreFlag) && p.t_off + p.n > P->pool_bytes))
       return fail(SF_ERR_INVALID, "job sequence outside the pool");
+    if ((p.t_off & kStoreFlag) && !ctx->store)
+      return fail(SF_ERR_INVALID, "store text but the context uses no store");
     keys.push_back({p.p_off, p.m, (uint32_t)(2 * q)});
     keys.push_back({p.t_off, p.n, (uint32_t)(2 * q + 1)});
   }
@@ -233,6 +236,7 @@ int plan_build(sf_plan* P) {
   items.reserve(np);
   const bool use16 = allow16();
   const TuneTable* tune = P->tune_override ? P->tune_override : &ctx->tune;
+  P->store = ctx->store;
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
@@ -502,6 +506,7 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
     pl.len = reinterpret_cast<const uint32_t*>(P->d_seq.as<uint8_t>() + nseq * 16);
     pl.nseq = (uint32_t)nseq;
     pl.pool = P->d_pool.as<uint32_t>();
+    pl.store = P->store ? P->store->words.as<uint32_t>() : nullptr;
     CK(sfk::launch_pack(pl, s));
     launches += nseq ? 1 : 0;
   }
@@ -781,7 +786,8 @@ Pass affine_pass(uint64_t p_off, uint64_t m, uint64_t t_off, uint64_t n, int mod
 }
 
 int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
-                          uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps) {
+                          uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps,
+                          const sf_store* store) {
   ps.clear();
   ps.reserve(count);
   for (uint64_t q = 0; q < count; ++q) {
@@ -792,8 +798,17 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
     p.m = j.m;
     p.n = j.n;
     if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
-    if (j.p_off + j.m > pool_bytes || j.t_off + j.n > pool_bytes)
+    if (j.text_src > SF_TEXT_STORE) return fail(SF_ERR_INVALID, "bad text source");
+    if (j.p_off > pool_bytes || j.m > pool_bytes - j.p_off)
       return fail(SF_ERR_INVALID, "job sequence outside the pool");
+    if (j.text_src == SF_TEXT_STORE) {
+      if (!store) return fail(SF_ERR_INVALID, "store text but the context uses no store");
+      if (j.t_off > store->bases || j.n > store->bases - j.t_off)
+        return fail(SF_ERR_INVALID, "text window outside the store");
+      p.t_off = kStoreFlag | (j.t_off + kStorePad);
+    } else if (j.t_off > pool_bytes || j.n > pool_bytes - j.t_off) {
+      return fail(SF_ERR_INVALID, "job sequence outside the pool");
+    }
     if (j.kind != SF_JOB_MYERS) {
       if (j.sc_index >= n_scores || !ok_sc(&scores[j.sc_index]))
         return fail(SF_ERR_INVALID, "bad scoring index");
@@ -1274,7 +1289,7 @@ int sf_plan_create(sf_context* ctx, const sf_job_t* jobs, uint64_t count, const 
   std::unique_ptr<sf_plan> P(new sf_plan);
   P->ctx = ctx;
   P->pool_bytes = pool_bytes;
-  int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes);
+  int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes, ctx->store);
   if (rc) return rc;
   if ((rc = plan_build(P.get()))) return rc;
   *out = P.release();
@@ -1507,7 +1522,7 @@ int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, cons
     ctx->cache->ctx = ctx;
   }
   sf_plan* P = ctx->cache.get();
-  int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes);
+  int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes, ctx->store);
   if (rc) return rc;
   P->pool_bytes = pool_bytes;
   if ((rc = plan_build(P))) return rc;
@@ -1671,6 +1686,73 @@ int sf_plan_tune(sf_plan* P, const uint8_t* pool, uint32_t reps, char* report, u
 int sf_context_untune(sf_context* ctx) {
   if (!ctx) return fail(SF_ERR_INVALID, "null context");
   ctx->tune.clear();
+  return SF_OK;
+}
+
+// ---- transcript store ---------------------------------------------------------------
+
+int sf_store_create(sf_context* ctx, const uint8_t* codes, const uint64_t* lens, uint64_t count,
+                    sf_store** out) {
+  if (!ctx || !out || (count && !lens)) return fail(SF_ERR_INVALID, "bad argument");
+  uint64_t bases = 0;
+  for (uint64_t q = 0; q < count; ++q) bases += lens[q];
+  if (bases && !codes) return fail(SF_ERR_INVALID, "null codes");
+  CK(cudaSetDevice(ctx->dev));
+  std::unique_ptr<sf_store> S(new sf_store);
+  S->dev = ctx->dev;
+  S->bases = bases;
+  const uint64_t nwords = (bases + 15) / 16 + 1;
+  int rc = S->words.ensure((nwords + 64) * 4);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(S->words.p, 0, (nwords + 64) * 4, ctx->s));
+  if (bases) {
+    DevBuf staging;
+    if ((rc = staging.ensure(bases))) return rc;
+    CK(cudaMemcpyAsync(staging.p, codes, bases, cudaMemcpyHostToDevice, ctx->s));
+    CK(sfk::launch_store_pack(staging.as<uint8_t>(), bases, S->words.as<uint32_t>(), ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+  } else {
+    CK(cudaStreamSynchronize(ctx->s));
+  }
+  *out = S.release();
+  return SF_OK;
+}
+
+int sf_store_create_packed(sf_context* ctx, const uint64_t* tx_seq, uint64_t bases,
+                           sf_store** out) {
+  if (!ctx || !out || (bases && !tx_seq)) return fail(SF_ERR_INVALID, "bad argument");
+  CK(cudaSetDevice(ctx->dev));
+  std::unique_ptr<sf_store> S(new sf_store);
+  S->dev = ctx->dev;
+  S->bases = bases;
+  const uint64_t nwords = (bases + 15) / 16 + 1;
+  int rc = S->words.ensure((nwords + 64) * 4);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(S->words.p, 0, (nwords + 64) * 4, ctx->s));
+  // 32 bases per u64, read as two little-endian u32 words of 16: the store's own order.
+  if (bases)
+    CK(cudaMemcpyAsync(S->words.as<uint32_t>() + kStorePad / 16, tx_seq, (bases + 31) / 32 * 8,
+                       cudaMemcpyHostToDevice, ctx->s));
+  CK(cudaStreamSynchronize(ctx->s));
+  *out = S.release();
+  return SF_OK;
+}
+
+void sf_store_destroy(sf_store* store) {
+  if (!store) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(store->dev);
+  delete store;
+  cudaSetDevice(prev);
+}
+
+uint64_t sf_store_bases(const sf_store* store) { return store ? store->bases : 0; }
+
+int sf_context_use_store(sf_context* ctx, sf_store* store) {
+  if (!ctx) return fail(SF_ERR_INVALID, "null context");
+  if (store && store->dev != ctx->dev) return fail(SF_ERR_INVALID, "store on another device");
+  ctx->store = store;
   return SF_OK;
 }
 

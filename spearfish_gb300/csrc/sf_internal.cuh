@@ -176,6 +176,8 @@ cudaError_t launch_myers(int blocks_per_lane, const MyersLaunch& a, int grid, in
 extern const int kMyersB[];
 extern const int kMyersNB;
 
+// Sequences of a batch into its packed pool: from the byte pool, or (byte_off with bit 63
+// set) sliced from the transcript store's packed words at that base position.
 struct PackLaunch {
   const uint8_t* bytes;
   const uint64_t* byte_off;  // per sequence
@@ -183,7 +185,11 @@ struct PackLaunch {
   const uint64_t* word_off;
   uint32_t nseq;
   uint32_t* pool;
+  const uint32_t* store;     // transcript store words (may be null)
 };
+// Byte codes -> store words: base p at position p + 16 (one leading word of padding).
+cudaError_t launch_store_pack(const uint8_t* codes, uint64_t bases, uint32_t* words,
+                              cudaStream_t s);
 cudaError_t launch_pack(const PackLaunch& a, cudaStream_t s);
 
 // Exclusive scan of per-job op counts (single block) and the gather that compacts ops.

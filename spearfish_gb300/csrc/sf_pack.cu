@@ -11,10 +11,25 @@ __global__ void __launch_bounds__(256) pack_kernel(sfk::PackLaunch a) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t s = warp; s < a.nseq; s += nwarps) {
-    const uint8_t* src = a.bytes + a.byte_off[s];
+    const uint64_t off = a.byte_off[s];
     const uint64_t len = a.len[s];
     const uint64_t words = (len + 1 + 15) / 16;  // one leading pad base
     uint32_t* dst = a.pool + a.word_off[s];
+    if (off >> 63) {
+      // A window of the transcript store: packed base x (x >= 1) is store position
+      // pos + x - 1; the pad base takes the store base before the window (never matched).
+      const uint64_t pos = (off & ~(uint64_t(1) << 63)) - 1;
+      for (uint64_t w = lane; w < words; w += 32) {
+        const uint64_t b0 = pos + 16 * w, wi = b0 >> 4;
+        uint32_t v = __funnelshift_r(__ldg(a.store + wi), __ldg(a.store + wi + 1),
+                                     2u * (uint32_t)(b0 & 15));
+        const uint64_t valid = len + 1 - 16 * w;  // bases of this word inside the window
+        if (valid < 16) v &= (1u << (2 * valid)) - 1u;
+        dst[w] = v;
+      }
+      continue;
+    }
+    const uint8_t* src = a.bytes + off;
     for (uint64_t w = lane; w < words; w += 32) {
       uint32_t v = 0;
 #pragma unroll
@@ -88,9 +103,35 @@ __global__ void __launch_bounds__(256) gather_kernel(const sf::TRes* tres, const
   }
 }
 
+// Store words from byte codes: word w holds positions 16w .. 16w + 15, base p at p + 16.
+__global__ void __launch_bounds__(256) store_pack_kernel(const uint8_t* codes, uint64_t bases,
+                                                         uint64_t nwords, uint32_t* words) {
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t v = 0;
+    if (w > 0) {
+#pragma unroll
+      for (int b = 0; b < 16; ++b) {
+        const uint64_t p = 16 * (w - 1) + b;
+        if (p < bases) v |= (uint32_t)(codes[p] & 3) << (2 * b);
+      }
+    }
+    words[w] = v;
+  }
+}
+
 }  // namespace
 
 namespace sfk {
+
+cudaError_t launch_store_pack(const uint8_t* codes, uint64_t bases, uint32_t* words,
+                              cudaStream_t s) {
+  const uint64_t nwords = (bases + 15) / 16 + 1;
+  const uint64_t blocks = (nwords + 255) / 256;
+  store_pack_kernel<<<(unsigned)(blocks < 152u * 32u ? blocks : 152u * 32u), 256, 0, s>>>(
+      codes, bases, nwords, words);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_pack(const PackLaunch& a, cudaStream_t s) {
   if (a.nseq == 0) return cudaSuccess;
