@@ -291,10 +291,20 @@ def run_serving(args, ws, rank, local):
     stream = W.serving_stream(args.serve_seconds, seed=5 + rank)
     rng = np.random.default_rng(505 + rank)
     batches = []
+    store = ctx = tx = None
+    if args.store:
+        # The transcripts live in HBM for the whole stream; requests carry reads only.
+        tx = W.Transcriptome()
+        ctx = B.Context(local)
+        store = B.Store(ctx, tx.txs)
     for _, size in stream:
-        reads = [W.serving_read(rng, hifi=rng.random() < 0.1) for _ in range(size)]
-        batches.append(W.serving_jobs(reads, B))
-    srv = S.Server(local, slots=args.slots)
+        if store is not None:
+            reads = [W.serving_store_read(tx, rng, hifi=rng.random() < 0.1) for _ in range(size)]
+            batches.append(W.serving_store_jobs(tx, reads, B))
+        else:
+            reads = [W.serving_read(rng, hifi=rng.random() < 0.1) for _ in range(size)]
+            batches.append(W.serving_jobs(reads, B))
+    srv = S.Server(local, slots=args.slots, store=store)
     try:
         for pool, jobs in batches[:3]:  # warm-up: buffers grow to a working size
             srv.wait(srv.submit(pool, jobs))
@@ -340,6 +350,9 @@ def run_serving(args, ws, rank, local):
         q = srv.query()
     finally:
         srv.close()
+        if store is not None:
+            store.close()
+            ctx.close()
     if rank == 0:
         line = {"metric": "alignment GCUPS", "value": sat["gcups"], "unit": "GCUPS",
                 "n_gpus": ws, "steps": 1, "warmup": 3, "ms_per_step": wall2 * 1e3,
@@ -347,6 +360,8 @@ def run_serving(args, ws, rank, local):
                 "dtype": "int32", "data": "synthetic (seeded read model; sim.rs error model)",
                 "config": {"workload": GOLD["c5"], "serve_seconds": args.serve_seconds,
                            "slots": args.slots, "jobs_per_read": 4,
+                           "texts": "transcript store (HBM), windows sliced on the device"
+                           if store is not None else "in each request's pool",
                            "parallelism": f"replicas x{ws}"},
                 "latency": live, "saturation": sat,
                 "server": {k: int(v) for k, v in q.items()},
@@ -366,6 +381,9 @@ def main():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="c5: stream length")
     ap.add_argument("--slots", type=int, default=8, help="c5: requests on the device at once")
+    ap.add_argument("--store", type=int, default=1,
+                    help="c5: texts as windows of a device-resident transcript store (1) or in "
+                         "each request's pool (0)")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload's pairs")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)

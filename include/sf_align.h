@@ -368,6 +368,7 @@ typedef struct {
     uint64_t hbm_budget;  /* bytes the slots may hold (0: 90% of free memory) */
     const sf_affine_t *scores; /* scoring table for sc_index (NULL: ONT) */
     uint32_t n_scores;
+    sf_store *store;      /* transcript store for SF_TEXT_STORE texts (may be NULL) */
 } sf_server_opts;
 
 typedef struct {

@@ -71,7 +71,7 @@ class ResultT(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("slots", C.c_uint32), ("hbm_budget", C.c_uint64),
-                ("scores", C.POINTER(Affine)), ("n_scores", C.c_uint32)]
+                ("scores", C.POINTER(Affine)), ("n_scores", C.c_uint32), ("store", C.c_void_p)]
 
 
 class RequestStats(C.Structure):

@@ -66,6 +66,7 @@ struct Slot {
 struct sf_server {
   int dev = 0;
   uint64_t budget = 0;
+  sf_store* store = nullptr;  // transcript store for SF_TEXT_STORE texts
   std::vector<sf_affine_t> scores;
   std::vector<Slot> slots;
   std::mutex mu;
@@ -227,6 +228,9 @@ int sf_server_create(const sf_server_opts* opts, sf_server** out) {
     return fail(SF_ERR_INVALID, "bad argument");
   std::unique_ptr<sf_server> S(new sf_server);
   S->dev = opts->device;
+  if (opts->store && opts->store->dev != opts->device)
+    return fail(SF_ERR_INVALID, "store on another device");
+  S->store = opts->store;
   const uint32_t slots = opts->slots ? std::min<uint32_t>(opts->slots, 64) : 8;
   for (uint32_t q = 0; q < opts->n_scores; ++q) S->scores.push_back(opts->scores[q]);
   if (S->scores.empty()) S->scores.push_back(sf_affine_t{2, 4, 4, 2});
@@ -234,6 +238,7 @@ int sf_server_create(const sf_server_opts* opts, sf_server** out) {
     Slot sl;
     int rc = make_context(S->dev, &sl.ctx);
     if (rc) return rc;
+    sl.ctx->store = S->store;
     sl.plan.reset(new sf_plan);
     sl.plan->ctx = sl.ctx;
     sl.plan->owns_ctx = true;
@@ -272,7 +277,7 @@ int sf_server_submit(sf_server* S, const uint8_t* pool, uint64_t pool_bytes, con
     return fail(SF_ERR_INVALID, "bad argument");
   auto req = std::make_shared<Request>();
   int rc = jobs_to_passes(jobs, count, S->scores.data(), (uint32_t)S->scores.size(), pool_bytes,
-                          req->passes);
+                          req->passes, S->store);
   if (rc) return rc;
   req->pool = pool;
   req->pool_bytes = pool_bytes;

@@ -31,11 +31,12 @@ class Stats:
 
 class Server:
     def __init__(self, device: int = 0, slots: int = 8, hbm_budget: int = 0,
-                 scores: Sequence = (Affine.ONT,)):
+                 scores: Sequence = (Affine.ONT,), store=None):
         self._lib = _abi.load()
         self._scores = (_abi.Affine * max(1, len(scores)))(*[_aff(s) for s in scores])
+        self._store = store  # jobs may name texts as windows of it (text_src = TEXT_STORE)
         opts = _abi.ServerOpts(int(device), int(slots), int(hbm_budget), self._scores,
-                               len(scores))
+                               len(scores), store.handle if store is not None else None)
         h = C.c_void_p()
         _abi.check(self._lib.sf_server_create(C.byref(opts), C.byref(h)))
         self.handle = h

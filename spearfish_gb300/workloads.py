@@ -244,6 +244,86 @@ def serving_jobs(reads: list, B) -> tuple[np.ndarray, np.ndarray]:
     return (np.concatenate(pool) if pool else np.zeros(1, np.uint8)), jobs
 
 
+class Transcriptome:
+    """Seeded transcripts for the served stream over the transcript store: ONT-like
+    transcripts of 300..12,000 bases (log-normal, median 1,500) and, for the HiFi-like 10%,
+    longer ones of 1..20 kb.  `starts` are their first bases in the concatenation (as the
+    index's `tx_range` numbers them)."""
+
+    def __init__(self, n_ont: int = 20_000, n_long: int = 1_000, seed: int = 55):
+        rng = np.random.default_rng(seed)
+        lens = np.clip(np.exp(np.log(1500.0) + 0.6 * rng.standard_normal(n_ont)), 300, 12000)
+        self.ont = [rng.integers(0, 4, int(L), dtype=np.uint8) for L in lens]
+        self.long = [rng.integers(0, 4, int(rng.integers(1000, 20001)), dtype=np.uint8)
+                     for _ in range(n_long)]
+        self.txs = self.ont + self.long
+        sizes = np.array([t.size for t in self.txs], dtype=np.uint64)
+        self.starts = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+
+
+def serving_store_read(tx: Transcriptome, rng: np.random.Generator, hifi: bool):
+    """A read of the served stream drawn from a stored transcript: ONT cDNA-like reads cover
+    the transcript's 3' end (the reference simulator keeps the 3' end,
+    crates/spearfish-cli/src/simulate_cmd.rs:4-6) at 7% error; HiFi-like reads cover a long
+    transcript at 1%.  Returns (read codes, transcript index, region start, region end)."""
+    if hifi:
+        x = len(tx.ont) + int(rng.integers(0, len(tx.long)))
+        t = tx.txs[x]
+        a, b = 0, t.size
+        read = simulate(t, 0.01, HIFI, rng)
+    else:
+        x = int(rng.integers(0, len(tx.ont)))
+        t = tx.txs[x]
+        a, b = t.size - int(t.size * rng.uniform(0.5, 1.0)), t.size
+        read = simulate(t[a:b], 0.07, ONT_CDNA, rng)
+    return read, x, a, b
+
+
+def serving_store_jobs(tx: Transcriptome, reads: list, B) -> tuple[np.ndarray, np.ndarray]:
+    """`serving_jobs` with the texts named as windows of the transcript store: the Myers
+    Infix distance against the region with up to 50 transcript bases either side, the banded
+    Global pass over the region and the right-end extension read their text from the store;
+    only the reads (and the reversed left-end window, which the store holds forwards) go in
+    the request's pool."""
+    pool, at, rows = [], 0, []
+
+    def put(a):
+        nonlocal at
+        pool.append(a)
+        off = at
+        at += a.size
+        return off
+
+    S, P = B.TEXT_STORE, B.TEXT_POOL
+    for read, x, a, b in reads:
+        t = tx.txs[x]
+        s0 = int(tx.starts[x])
+        m = read.size
+        po = put(read)
+        fa, fb = max(0, a - 50), min(t.size, b + 50)
+        rows.append((po, m, s0 + fa, fb - fa, S, B.JOB_MYERS, 0, 0, 0, 0, 0, 0))
+        band = int(c3_band(np.array([float(m)]))[0])
+        rows.append((po, m, s0 + a, b - a, S, B.JOB_AFFINE, 2, 1, band, 0, 0, 0))
+        xr = min(100, m)
+        w = xr + 20 + xr // 10
+        ta = max(a, b - w)
+        rows.append((po + m - xr, xr, s0 + ta, b - ta, S, B.JOB_EXTEND_WINDOW, 1, 1, 16, w, 5, 50))
+        head_r = np.ascontiguousarray(read[:xr][::-1])
+        head_t = np.ascontiguousarray(t[a:min(b, a + w)][::-1])
+        rows.append((put(head_r), xr, put(head_t), head_t.size, P, B.JOB_EXTEND_WINDOW, 1, 1, 16,
+                     w, 5, 50))
+    jobs = B.new_jobs(len(rows))
+    for q, (po, m, to, n, src, kind, mode, cig, band, win, bonus, xd) in enumerate(rows):
+        j = jobs[q]
+        j["p_off"], j["m"], j["t_off"], j["n"], j["text_src"] = po, m, to, n, src
+        j["kind"], j["mode"], j["want_cigar"] = kind, mode, cig
+        if kind != B.JOB_MYERS:
+            j["band"] = band
+        if kind == B.JOB_EXTEND_WINDOW:
+            j["window"], j["end_bonus"], j["xdrop"] = win, bonus, xd
+    return (np.concatenate(pool) if pool else np.zeros(1, np.uint8)), jobs
+
+
 def serving_stream(duration_s: float, reads_per_s: float = 2000.0, burst: float = 5.0,
                    max_batch: int = 4096, seed: int = 5):
     """Arrivals of read batches: batch sizes log-uniform over 1..max_batch reads, batch

@@ -132,3 +132,42 @@ def test_errors_and_bounded_waits(mods):
         assert len(r[0].results) == len(jobs)
     finally:
         srv.close()
+
+
+def test_store_requests_equal_pool_requests(mods):
+    """Requests whose texts are windows of the server's transcript store give the same
+    results as the same requests with the windows' codes in their pools."""
+    B, S, W = mods
+    tx = W.Transcriptome(n_ont=300, n_long=20, seed=56)
+    rng = np.random.default_rng(57)
+    reqs = []
+    for _ in range(6):
+        reads = [W.serving_store_read(tx, rng, hifi=rng.random() < 0.1)
+                 for _ in range(int(rng.integers(1, 30)))]
+        reqs.append(W.serving_store_jobs(tx, reads, B))
+    cat = np.concatenate(tx.txs)
+
+    def copied(pool, jobs):
+        parts, at = [pool], pool.size
+        j2 = jobs.copy()
+        for q in range(len(jobs)):
+            if jobs["text_src"][q] == B.TEXT_STORE:
+                o, n = int(jobs["t_off"][q]), int(jobs["n"][q])
+                parts.append(cat[o:o + n])
+                j2["t_off"][q], j2["text_src"][q] = at, B.TEXT_POOL
+                at += n
+        return np.concatenate(parts), j2
+
+    ctx = B.Context(0)
+    store = B.Store(ctx, tx.txs)
+    srv = S.Server(0, slots=3, store=store)
+    try:
+        tickets = [srv.submit(p, j) for p, j in reqs]
+        got = [srv.wait(t)[0] for t in tickets]
+        want = [srv.wait(srv.submit(*copied(p, j)))[0] for p, j in reqs]
+        for a, b in zip(got, want):
+            _same(a, b)
+    finally:
+        srv.close()
+        store.close()
+        ctx.close()
