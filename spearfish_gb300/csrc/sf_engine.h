@@ -178,10 +178,8 @@ struct sf_plan {
   const sf_store* store = nullptr;
   // Class overrides for this plan only (the autotuner's trial plans); else the context's.
   const sfe::TuneTable* tune_override = nullptr;
-  ~sf_plan() {
-    if (graph) cudaGraphExecDestroy(graph);
-    if (owns_ctx) delete ctx;
-  }
+  // Out of line (sf_host.cu): deleting an owned context needs sf_context complete.
+  ~sf_plan();
 };
 
 // ---- context ---------------------------------------------------------------------------

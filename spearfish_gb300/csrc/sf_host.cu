@@ -162,6 +162,15 @@ DJob make_djob(const Pass& p, uint32_t& flags) {
   return j;
 }
 
+}  // namespace sfe
+
+sf_plan::~sf_plan() {
+  if (graph) cudaGraphExecDestroy(graph);
+  if (owns_ctx) delete ctx;
+}
+
+namespace sfe {
+
 uint64_t seq_words(uint64_t len) { return (len + 1 + 15) / 16; }
 
 // Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
