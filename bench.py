@@ -153,6 +153,7 @@ def workload(cfg: str, scale: float, cigar: bool = True):
 
 AFFINE_C = (4, 6, 8, 9, 10, 11, 12, 14, 16, 20, 24, 28, 32, 40, 48)  # 32-bit register classes
 AFFINE16_C = (4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48, 56, 64)  # packed 16-bit classes
+AFFINE16H_C = (8, 10, 12, 14, 16, 18, 20, 24)  # the same with 16 lanes a pass
 
 
 def fits16(j, w, sc, B) -> bool:
@@ -195,10 +196,15 @@ def job_classes(jobs, B, scores=((2, 4, 4, 2),)):
         w = max(0, min(w, n + 1))
         tbf = bool(j["want_cigar"]) and j["kind"] != B.JOB_LOCAL
         if fits16(j, w, scores[int(j["sc_index"])], B):
-            out.append(("affine16", next(c for c in AFFINE16_C if 32 * c >= w), False, tbf))
+            if os.environ.get("SF_AFFINE16_LANES") == "16" and w <= 16 * AFFINE16H_C[-1]:
+                out.append(("affine16", next(c for c in AFFINE16H_C if 16 * c >= w), False, tbf,
+                            16))
+            else:
+                out.append(("affine16", next(c for c in AFFINE16_C if 32 * c >= w), False, tbf,
+                            32))
             continue
         c = next((c for c in AFFINE_C if 32 * c >= w), None)
-        out.append(("affine", c, False, tbf) if c else ("affine", 16, True, tbf))
+        out.append(("affine", c, False, tbf, 32) if c else ("affine", 16, True, tbf, 32))
     return out
 
 
@@ -423,10 +429,10 @@ def main():
     tune_map = {}
     for g in (tune_report or {}).get("groups", []):
         key = ("myers", g["c"], g["lanes"]) if g["kind"] == "myers" else \
-            (g["kind"], g["c"], bool(g["wide"]), bool(g["traceback"]))
+            (g["kind"], g["c"], bool(g["wide"]), bool(g["traceback"]), g["lanes"])
         ch = g["chosen"]
         tune_map[key] = ("myers", ch["c"], ch["lanes"]) if g["kind"] == "myers" else \
-            (g["kind"], ch["c"], bool(g["wide"]), bool(g["traceback"]))
+            (g["kind"], ch["c"], bool(g["wide"]), bool(g["traceback"]), ch["lanes"])
     stream = torch.cuda.ExternalStream(plan.stream(), device=local)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB
     for _ in range(args.warmup):
@@ -471,7 +477,7 @@ def main():
     tb = desc["buckets"][top - 1]
     cls = [tune_map.get(c, c) for c in job_classes(jobs, B)]
     key = ("myers", tb["c"], tb["lanes"]) if tb["kind"] == "myers" else \
-        (tb["kind"], tb["c"], bool(tb["wide"]), bool(tb["traceback"]))
+        (tb["kind"], tb["c"], bool(tb["wide"]), bool(tb["traceback"]), tb["lanes"])
     sel = np.array([c == key for c in cls])
     top_cells = int(out.results["cells"][sel].astype(np.uint64).sum())
     ops_cell = OPS_PER_CELL["myers"] if tb["kind"] == "myers" else (

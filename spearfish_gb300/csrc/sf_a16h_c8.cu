@@ -1,0 +1,9 @@
+// Half-warp packed 16-bit banded affine kernels: 16 lanes a pass, C = 8 cells per lane
+// (4 words; bands up to 128 cells), two passes per warp.
+#include "sf_affine16_impl.cuh"
+
+namespace sfk {
+cudaError_t launch_affine16h_8(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {
+  return launch_affine16h_c<4>(tb, a, grid, block, s);
+}
+}  // namespace sfk

@@ -44,4 +44,31 @@ cudaError_t launch_affine16(int c, bool tb, const AffLaunch& a, int grid, int bl
   }
 }
 
+cudaError_t launch_affine16h_8(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_10(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_12(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_14(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_16(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_18(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_20(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16h_24(bool, const AffLaunch&, int, int, cudaStream_t);
+
+const int kAffine16HC[] = {8, 10, 12, 14, 16, 18, 20, 24};
+const int kAffine16HNC = 8;
+
+cudaError_t launch_affine16h(int c, bool tb, const AffLaunch& a, int grid, int block,
+                             cudaStream_t s) {
+  switch (c) {
+    case 8: return launch_affine16h_8(tb, a, grid, block, s);
+    case 10: return launch_affine16h_10(tb, a, grid, block, s);
+    case 12: return launch_affine16h_12(tb, a, grid, block, s);
+    case 14: return launch_affine16h_14(tb, a, grid, block, s);
+    case 16: return launch_affine16h_16(tb, a, grid, block, s);
+    case 18: return launch_affine16h_18(tb, a, grid, block, s);
+    case 20: return launch_affine16h_20(tb, a, grid, block, s);
+    case 24: return launch_affine16h_24(tb, a, grid, block, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace sfk

@@ -434,6 +434,362 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   __syncwarp();
 }
 
+// ---------------------------------------------------------------------------------------
+// Half-warp passes: the same rows with 16 lanes to a pass and two passes to a warp, so that a
+// row's fixed costs (the gap scan, the neighbour shuffles, table and bookkeeping work) are
+// shared between the warp's two passes and a lane holds twice the cells.  Lane l of segment
+// s = lane / 16 holds offsets [(l % 16) * C, (l % 16) * C + C) of its own pass.  The two
+// passes run their rows in lockstep; each keeps its own geometry, band shift, offset and
+// bookkeeping, and a pass that has ended (or stopped) computes on without storing until its
+// partner ends.
+
+// Maximum over the 16 lanes of a segment.
+__device__ __forceinline__ uint32_t seg_max(uint32_t v) {
+#pragma unroll
+  for (int s = 8; s >= 1; s >>= 1) v = max(v, __shfl_xor_sync(FULL, v, s, 16));
+  return v;
+}
+
+// Leftmost offset holding field v in the lane's segment (some lane of it holds it).
+template <int C2>
+__device__ __forceinline__ uint32_t seg_leftmost(const uint32_t (&h)[C2], uint32_t v, int lane) {
+  constexpr int C = 2 * C2;
+  int cf = C;
+#pragma unroll
+  for (int c = C - 1; c >= 0; --c) {
+    const uint32_t u = c < C2 ? (h[c] & 0xffffu) : (h[c - C2] >> 16);
+    if (u == v) cf = c;
+  }
+  const uint32_t bal = (__ballot_sync(FULL, cf < C) >> (lane & 16)) & 0xffffu;
+  const int src = __ffs(bal) - 1;
+  const int cs = __shfl_sync(FULL, cf, src < 0 ? 0 : src, 16);
+  return (uint32_t)(src < 0 ? 0 : src) * C + (uint32_t)cs;
+}
+
+template <int C2, bool TB>
+__device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lane) {
+  constexpr int P = 16;
+  constexpr int C = 2 * C2;
+  constexpr int G = (C2 + 7) / 8;
+  constexpr bool kMasks = C2 <= 8;
+  const int l = lane & 15;
+  const PassCtx x = make_ctx(a, jid);
+  const int32_t m = (int32_t)x.m, n = (int32_t)x.n;
+  const Geo32 g{(x.P.flags & F_FULL) != 0, false, clamp30(x.J.below), clamp30(x.J.above), n};
+  const int32_t cut =
+      x.cuton ? (int32_t)(x.J.cut < (uint64_t)n + 1 ? x.J.cut : (uint64_t)n + 1) : INT32_MAX;
+  const int32_t kb = l * C;
+  const uint32_t one = (uint32_t)opaque_one();
+  const uint32_t go2 = (uint32_t)x.go * kOne2;
+  const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;
+  const uint32_t ext2 = (uint32_t)x.ext * kOne2;
+  const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
+  const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
+  const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;
+  const int32_t dC = x.ext * C, dH = -x.ext * C2;
+  const int32_t goX = x.go + x.ext * (C2 - 1);
+  const int32_t e_lane = (int32_t)kNeg16 - dC * l;
+  int32_t off = -(int32_t)kBias16;
+  uint32_t h[C2], f[C2], sel[C2], smask[kMasks ? C2 : 1];
+  int32_t plo, phi;
+  g.range(0, plo, phi);
+  {
+    const int32_t w0 = phi - plo + 1;
+#pragma unroll
+    for (int k = 0; k < C2; ++k) {
+      const int32_t K = kb + k, K2 = kb + C2 + k;
+      const uint32_t lo = K < w0 ? (uint32_t)(row0_value(x, plo + K) - off) : kNeg16;
+      const uint32_t hi = K2 < w0 ? (uint32_t)(row0_value(x, plo + K2) - off) : kNeg16;
+      h[k] = pk2(lo, hi);
+      f[k] = kNeg2;
+    }
+  }
+  {
+    int32_t lo1, hi1;
+    g.range(1, lo1, hi1);
+    Win<C> win;
+    win.load(a.pool, x.J.t_word, lo1 + kb);
+#pragma unroll
+    for (int k = 0; k < C2; ++k) sel[k] = sel_byte(win.at(k)) | (sel_byte(win.at(C2 + k)) << 8);
+  }
+  int32_t Wm = -1;
+  auto set_masks = [&](int32_t W) {
+    const int32_t c = W - kb;
+#pragma unroll
+    for (int k = 0; k < (kMasks ? C2 : 1); ++k)
+      smask[k] = (c == k ? 0xffffu : 0u) | (c == C2 + k ? 0xffff0000u : 0u);
+    Wm = W;
+  };
+  Book b;
+  uint32_t pw = m > 0 ? __ldg(a.pool + x.J.p_word) >> 2 : 0;
+  uint2* tb0 = TB ? reinterpret_cast<uint2*>(a.tb + x.J.tb_word) + l : nullptr;
+  // This pass's rows: 1 .. endA keep lo = 0; endA + 1 .. endB move it; rows past n + below
+  // are empty (the pass ends there with no score).  The warp runs to its longer pass's end.
+  const int32_t endA = m < g.below ? m : g.below;
+  const int64_t lastB = (int64_t)n + g.below;
+  const int32_t endB = (int64_t)m < lastB ? m : (int32_t)lastB;
+  const int32_t endA2 = max(endA, __shfl_xor_sync(FULL, endA, 16));
+  const int32_t endW = max(endB, __shfl_xor_sync(FULL, endB, 16));
+  int32_t fin = has ? 0 : -1;  // 0: running; > 0 ended at that row; -1: nothing to store
+  DRes r{};
+
+  // The pass's result from its last row i (band [lo, hi], values in h).  Every lane of the
+  // warp runs it (segment shuffles); a lane keeps it only for its own ending pass.
+  auto result = [&](int32_t i, int32_t lo, int32_t hi) {
+    const int32_t W = hi - lo + 1;
+    DRes q{};
+    q.clip_best = b.clip_best;
+    q.cut_best = b.cut_best;
+    q.clip_i = b.ci;
+    q.clip_j = b.cj;
+    q.text_read = (uint32_t)hi;
+    q.last_row = (uint32_t)m;
+    q.rows = (uint32_t)m;
+    q.cells = band_cells(m, g.below, g.above, n);
+    const int32_t K = n - lo;
+    const uint32_t u = __shfl_sync(FULL, field_at(h, K % C), (K / C) & 15, 16);
+    const uint32_t rmu = seg_max(lane_max16(h, kb, W));
+    const uint32_t lm = seg_leftmost(h, rmu, lane);
+    const int32_t lim = min(hi, cut) - lo + 1;
+    const uint32_t cm = seg_max(lane_max16(h, kb, lim));
+    if (x.mode == 2) {
+      q.score = (int32_t)u + off;
+      q.score_col = (uint32_t)n;
+    } else {
+      q.score = (int32_t)rmu + off;
+      q.score_col = (uint32_t)(lo + lm);
+    }
+    q.cut_score = (x.cuton && lo <= cut) ? (int32_t)cm + off : NEG;
+    (void)i;
+    return q;
+  };
+
+  // One row of both passes.  MODE 1: both passes' lo moves right by one (compile time);
+  // MODE 0: per pass (d1), the rows before the band leaves column 0.
+  auto row = [&](int32_t i, auto modetag, bool d1) {
+    constexpr bool ALL1 = decltype(modetag)::value;
+    const bool D1 = ALL1 ? true : d1;
+    const bool act = fin == 0 && i <= endB;
+    const int32_t lo = D1 ? i - g.below : 0, hi = min(i + g.above, n);
+    const int32_t W = hi - lo + 1;
+    if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + ((i <= m ? i : m) >> 4));
+    const uint32_t pb = 8u * (pw & 3u);
+    pw >>= 2;
+    const uint32_t ta = (mpm & 0xffu) << pb, tbl = (mpm >> 8) << pb;
+    {
+      const uint32_t s0 = sel[0];
+      uint32_t nx = __shfl_down_sync(FULL, s0, 1, 16);
+      int32_t fc = lo + P * C - 1;
+      fc = fc < n ? fc : n;
+      const uint32_t far = sel_byte(base_at(a.pool, x.J.t_word, (uint64_t)(fc > 0 ? fc : 0)));
+      if (l == 15) nx = far;
+      const bool shift = D1 && i > 1;
+      const uint32_t last = __byte_perm(s0, nx, 0x2241);
+      if (ALL1) {
+        if (i > 1) {
+#pragma unroll
+          for (int k = 0; k + 1 < C2; ++k) sel[k] = sel[k + 1];
+          sel[C2 - 1] = last;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k + 1 < C2; ++k) sel[k] = shift ? sel[k + 1] : sel[k];
+        sel[C2 - 1] = shift ? last : sel[C2 - 1];
+      }
+    }
+    uint32_t nH = __shfl_down_sync(FULL, h[0], 1, 16), nF = __shfl_down_sync(FULL, f[0], 1, 16);
+    if (l == 15) nH = nF = kNeg2;
+    const uint32_t upH = __byte_perm(h[0], nH, 0x5432), upF = __byte_perm(f[0], nF, 0x5432);
+    uint32_t hdp = 0;
+    if (!ALL1) {
+      const uint32_t pl = __shfl_up_sync(FULL, h[C2 - 1], 1, 16);
+      hdp = __byte_perm(pl, h[C2 - 1], 0x5432);
+      if (l == 0) hdp = (hdp & 0xffff0000u) | (kNeg16 - (uint32_t)x.mat - 1u);
+    }
+    uint32_t red = 0, pend = 0;
+    uint32_t acc1[G];
+#pragma unroll
+    for (int q = 0; q < G; ++q) acc1[q] = 0;
+    sf_unroll<C2>([&](auto kt) {
+      constexpr int k = decltype(kt)::value;
+      const uint32_t hk = h[k], fk = f[k];
+      const uint32_t hu1 = k + 1 < C2 ? h[k + 1 < C2 ? k + 1 : 0] : upH;
+      const uint32_t fu1 = k + 1 < C2 ? f[k + 1 < C2 ? k + 1 : 0] : upF;
+      uint32_t hu, fu, hd;
+      if (ALL1) {
+        hu = hu1;
+        fu = fu1;
+        hd = hk;
+      } else {
+        hu = D1 ? hu1 : hk;
+        fu = D1 ? fu1 : fk;
+        hd = D1 ? hk : hdp;
+        hdp = hk;
+      }
+      const uint32_t ho = hu * one - go2;
+      const uint32_t fo = fu * one - ext2;
+      const uint32_t fj = __vmaxu2(ho, fo);
+      const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);
+      const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
+      if constexpr (TB)
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), xx - dgp + kGtDg);
+      const uint32_t t = ext2 * (uint32_t)k + xx;
+      if constexpr (k == 0)
+        red = t;
+      else if constexpr (k & 1)
+        pend = t;
+      else
+        red = __vimax3_u16x2(red, pend, t);
+      f[k] = fj;
+      h[k] = xx;
+    });
+    if constexpr (C2 % 2 == 0) red = __vmaxu2(red, pend);
+    const int32_t clo = (int32_t)(red & 0xffffu) - goX, chi = (int32_t)(red >> 16) - goX;
+    int32_t S = addmax(clo, dH, chi);
+    S = addmax(__shfl_up_sync(FULL, S, 1, 16), -dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 2, 16), -2 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 4, 16), -4 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 8, 16), -8 * dC, S);
+    const int32_t Sp = __shfl_up_sync(FULL, S, 1, 16);
+    const int32_t ein = l == 0 ? (int32_t)kNeg16 : max(e_lane, Sp);
+    const int32_t ehi = addmax(ein, dH, clo);
+    uint32_t e = pk2((uint32_t)ein, (uint32_t)ehi);
+    const uint32_t pl2 = __shfl_up_sync(FULL, h[C2 - 1], 1, 16);
+    uint32_t xp = __byte_perm(pl2, h[C2 - 1], 0x5432);
+    if (l == 0) xp = (xp & 0xffff0000u) | (kNeg16 - 1u);
+    uint32_t acc2[G];
+#pragma unroll
+    for (int q = 0; q < G; ++q) acc2[q] = 0;
+    sf_unroll<C2>([&](auto kt) {
+      constexpr int k = decltype(kt)::value;
+      const uint32_t xx = h[k];
+      const uint32_t xo = xp * one - go2;
+      if (k > 0) e = __viaddmax_u16x2(e, next2, xo);
+      if constexpr (TB) acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], gt2(e, xo), gt2(e, xx));
+      h[k] = __vmaxu2(xx, e);
+      xp = xx;
+    });
+    if constexpr (TB) {
+      if (act) {
+        uint2* tp = tb0 + (uint64_t)(i - 1) * (G * P);
+#pragma unroll
+        for (int q = 0; q < G; ++q) tp[q * P] = make_uint2(acc1[q], acc2[q]);
+      }
+    }
+    // Row bookkeeping (align.rs:2580-2640), each pass for itself; the segment shuffles run
+    // on every lane.
+    const bool want = act && x.rowmax_on;
+    const bool rebase = (i & (kRebaseRows - 1)) == 0;
+    if (__any_sync(FULL, want) || rebase) {
+      const uint32_t rmu = seg_max(lane_max16(h, kb, W));
+      const int32_t limc = (x.cuton && lo <= cut && hi > cut) ? cut - lo + 1 : W;
+      const uint32_t rcut = seg_max(lane_max16(h, kb, limc));
+      bool raise = false;
+      if (want) {
+        const int32_t rmax = (int32_t)rmu + off;
+        if (x.cuton && lo <= cut) b.cut_best = max(b.cut_best, (int32_t)rcut + off);
+        if (x.clip && rmax > b.clip_best) {
+          b.clip_best = rmax;
+          if (x.cell) {
+            b.ci = (uint32_t)i;
+            raise = true;
+          }
+        }
+      }
+      if (__any_sync(FULL, raise)) {
+        const uint32_t lm = seg_leftmost(h, rmu, lane);
+        if (raise) b.cj = (uint32_t)(lo + lm);
+      }
+      if (want && x.clip && (int32_t)rmu + off < sat_sub(b.clip_best, x.P.xdrop)) {
+        r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)hi, (uint32_t)i,
+                 (uint32_t)i, band_cells(i, g.below, g.above, n)};
+        fin = i;
+      }
+      if (rebase) {
+        const int32_t delta = (int32_t)rmu - (int32_t)kBias16;
+        const uint32_t dd = ((uint32_t)(-delta) & 0xffffu) * kOne2;
+#pragma unroll
+        for (int k = 0; k < C2; ++k) {
+          h[k] = __viaddmax_u16x2(h[k], dd, kNeg2);
+          f[k] = __viaddmax_u16x2(f[k], dd, kNeg2);
+        }
+        off += delta;
+      }
+    }
+    if (W < P * C) {
+      if constexpr (kMasks) {
+        if (W != Wm) set_masks(W);
+#pragma unroll
+        for (int k = 0; k < C2; ++k) {
+          h[k] = (h[k] & ~smask[k]) | (kNeg2 & smask[k]);
+          f[k] = (f[k] & ~smask[k]) | (kNeg2 & smask[k]);
+        }
+      } else if (l == W / C) {
+        set_neg16(h, f, W - kb);
+      }
+    }
+    const bool last = fin == 0 && i == endB;
+    if (__any_sync(FULL, last)) {
+      const DRes q = result(i, lo, hi);
+      if (last) {
+        r = endB < m ? DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n,
+                            (uint32_t)(endB + 1), (uint32_t)endB,
+                            band_cells(endB, g.below, g.above, n)}
+                     : q;
+        fin = i;
+      }
+    }
+    plo = lo;
+    phi = hi;
+  };
+
+  // Passes with no rows end at row 0 (m = 0: its row-0 values), or with an empty band
+  // before row 1 when n + below < 1 (no score).
+  const bool zero = fin == 0 && endB < 1;
+  if (__any_sync(FULL, zero)) {
+    const DRes q = result(0, plo, phi);
+    if (zero) {
+      r = m == 0 ? q
+                 : DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, 1u, 0u, 0ull};
+      if (m == 0) r.text_read = (uint32_t)phi;
+      fin = 0x7fffffff;
+    }
+  }
+  for (int32_t i = 1; i <= endA2; ++i) row(i, std::false_type{}, i > endA);
+  for (int32_t i = endA2 + 1; i <= endW; ++i) row(i, std::true_type{}, true);
+  if (has && l == 0) a.out[jid] = r;
+  if constexpr (TB) {
+    __syncwarp();
+    // Walk each segment's pass with the whole warp.
+    for (int s = 0; s < 2; ++s) {
+      const uint32_t js = __shfl_sync(FULL, jid, 16 * s);
+      const bool hs = __shfl_sync(FULL, (int)has, 16 * s) != 0;
+      if (!hs) continue;
+      const DJob Js = a.jobs[js];
+      const DParams Ps = a.params[js];
+      const DRes Rs = a.out[js];
+      walk_lean(a, js, tb_layout<C>(false, true, Js, Ps.flags, P), Js, Ps.flags, Rs, lane);
+      __syncwarp();
+    }
+  }
+  __syncwarp();
+}
+
+template <int C2, bool TB>
+__global__ void __launch_bounds__(128, (C2 == 8 || C2 >= 10) ? 3 : 4)
+    affine16h_kernel(sfk::AffLaunch a) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t q = 0;
+    if (lane == 0) q = atomicAdd(a.counter, 2u);
+    q = __shfl_sync(FULL, q, 0);
+    if (q >= a.njobs) break;
+    const uint32_t mine = q + (uint32_t)(lane >> 4);
+    const bool has = mine < a.njobs;
+    pair16h<C2, TB>(a, a.order[has ? mine : q], has, lane);
+  }
+}
+
 template <int C2>
 struct MinBlocks16 {
   static constexpr int value = C2 <= 8 ? 6 : (C2 <= 10 ? 4 : (C2 <= 16 ? 3 : 2));
@@ -454,6 +810,15 @@ __global__ void __launch_bounds__(128, MinBlocks16<C2>::value) affine16_kernel(s
 }  // namespace
 
 namespace sfk {
+
+template <int C2>
+cudaError_t launch_affine16h_c(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {
+  if (tb)
+    affine16h_kernel<C2, true><<<grid, block, 0, s>>>(a);
+  else
+    affine16h_kernel<C2, false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 template <int C2>
 cudaError_t launch_affine16_c(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {

@@ -93,12 +93,28 @@ bool allow16() {
   return !(env && env[0] == '0');
 }
 
+// Lanes per 16-bit pass by default: 32, or 16 (two passes per warp) with SF_AFFINE16_LANES=16
+// in the environment; the autotuner chooses per length bucket either way.
+int default_lanes16() {
+  const char* env = std::getenv("SF_AFFINE16_LANES");
+  return env && env[0] == '1' && env[1] == '6' ? 16 : 32;
+}
+
 // Kernel class of an affine or local pass: the packed 16-bit kernel when the pass fits it,
 // else the 32-bit register kernel, else (rows wider than 32 * 48 cells) the wide-row kernel.
 void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, PassKind& kind,
-                     int& c, bool& wide) {
+                     int& c, bool& wide, int& lanes, int lanes16 = 32) {
   wide = false;
+  lanes = 32;
   if (use16 && fits16(p, flags, wmax)) {
+    if (lanes16 == 16)
+      for (int q = 0; q < sfk::kAffine16HNC; ++q)
+        if (16 * (int64_t)sfk::kAffine16HC[q] >= wmax) {
+          kind = PK_AFFINE16;
+          c = sfk::kAffine16HC[q];
+          lanes = 16;
+          return;
+        }
     for (int q = 0; q < sfk::kAffine16NC; ++q)
       if (32 * (int64_t)sfk::kAffine16C[q] >= wmax) {
         kind = PK_AFFINE16;
@@ -244,6 +260,7 @@ int plan_build(sf_plan* P) {
   std::vector<std::pair<Key2, Item>> items;
   items.reserve(np);
   const bool use16 = allow16();
+  const int lanes16 = default_lanes16();
   const TuneTable* tune = P->tune_override ? P->tune_override : &ctx->tune;
   P->store = ctx->store;
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
@@ -275,17 +292,15 @@ int plan_build(sf_plan* P) {
     int c = 4;
     bool wide = false;
     PassKind kind = PK_AFFINE;
-    classify_affine(p, flags, wmax, use16, kind, c, wide);
+    int ln = 32;
+    classify_affine(p, flags, wmax, use16, kind, c, wide, ln, lanes16);
     const bool tb = p.want_cigar && p.kind != PK_LOCAL;
-    if (!wide) {
-      int ln = 32;
-      apply_tune(tune, kind, c, false, tb, ln);
-    }
+    if (!wide) apply_tune(tune, kind, c, false, tb, ln);
     if (tb) {
       flags |= F_TB;
       j.tb_word = tb_words;
       const int64_t chunks = wide ? wide_chunks(c, wmax) : 1;
-      tb_words += (uint64_t)p.m * tb_row_words(c, chunks);
+      tb_words += (uint64_t)p.m * (tb_row_words(c, chunks) * (uint64_t)ln / 32);
     }
     if (wide) scratch_cells = std::max<uint64_t>(scratch_cells, (uint64_t)wide_chunks(c, wmax) * 32 * c);
     DParams pr{};
@@ -309,7 +324,7 @@ int plan_build(sf_plan* P) {
     }
     P->slot[q] = (uint32_t)dj.size();
     const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
-    items.push_back({Key2{kind, c, wide, tb, 32}, Item{(uint32_t)dj.size(), work}});
+    items.push_back({Key2{kind, c, wide, tb, ln}, Item{(uint32_t)dj.size(), work}});
     dj.push_back(j);
     dp.push_back(pr);
     tj.push_back(t);
@@ -396,7 +411,8 @@ int plan_build(sf_plan* P) {
       b.grid = (int)std::min<uint64_t>((warps + wpb - 1) / wpb, (uint64_t)ctx->sms * (2048 / b.block));
     } else {
       b.block = 128;
-      const uint64_t blocks = (b.count + 3) / 4;
+      const uint64_t per_block = b.lanes == 16 ? 8 : 4;  // passes a 4-warp block holds
+      const uint64_t blocks = (b.count + per_block - 1) / per_block;
       const uint64_t cap = b.wide ? (uint64_t)ctx->sms * 2 : (uint64_t)ctx->sms * 16;
       b.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, cap));
       if (b.wide) {
@@ -559,7 +575,9 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
       al.tjobs = P->d_tjobs.as<TJob>();
       al.ops = P->d_ops.as<uint32_t>();
       al.tres = P->d_tres.as<TRes>();
-      if (b.kind == PK_AFFINE16)
+      if (b.kind == PK_AFFINE16 && b.lanes == 16)
+        CK(sfk::launch_affine16h(b.c, b.tb, al, b.grid, b.block, bs));
+      else if (b.kind == PK_AFFINE16)
         CK(sfk::launch_affine16(b.c, b.tb, al, b.grid, b.block, bs));
       else
         CK(sfk::launch_affine(b.c, b.wide, b.tb, b.kind == PK_LOCAL, al, b.grid, b.block, bs));
@@ -950,7 +968,8 @@ uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_byte
     int c = 4;
     bool wide = false;
     PassKind kind = PK_AFFINE;
-    classify_affine(p, flags, wmax, use16, kind, c, wide);
+    int ln = 32;
+    classify_affine(p, flags, wmax, use16, kind, c, wide, ln);
     if (p.want_cigar && p.kind != PK_LOCAL) {
       b += (uint64_t)p.m * tb_row_words(c, wide ? wide_chunks(c, wmax) : 1) * 4;
       b += 2 * ((uint64_t)p.m + p.n + 2) * 4;
@@ -1555,13 +1574,13 @@ int default_class(const Pass& p, bool use16, ClassKey& key, int64_t& blocks) {
   uint32_t flags = 0;
   DJob j = make_djob(p, flags);
   const int64_t wmax = band_wmax(j, flags);
-  int c = 4;
+  int c = 4, lanes = 32;
   bool wide = false;
   PassKind kind = PK_AFFINE;
-  classify_affine(p, flags, wmax, use16, kind, c, wide);
+  classify_affine(p, flags, wmax, use16, kind, c, wide, lanes, default_lanes16());
   const bool tb = p.want_cigar && p.kind != PK_LOCAL;
-  key = ClassKey{kind, c, wide ? 1 : 0, tb ? 1 : 0, 32};
-  blocks = 0;
+  key = ClassKey{kind, c, wide ? 1 : 0, tb ? 1 : 0, lanes};
+  blocks = wmax;  // affine: the group's widest row
   return SF_OK;
 }
 
@@ -1582,10 +1601,25 @@ std::vector<ClassChoice> tune_candidates(const ClassKey& key, int64_t blocks) {
       if (!dup) out.push_back(ClassChoice{b, lanes});
     }
   } else if (!key.wide) {
-    const int* cs = key.kind == PK_AFFINE16 ? sfk::kAffine16C : sfk::kAffineC;
-    const int nc = key.kind == PK_AFFINE16 ? sfk::kAffine16NC : sfk::kAffineNC;
+    const bool half = key.kind == PK_AFFINE16 && key.lanes == 16;
+    const int* cs = key.kind == PK_AFFINE16 ? (half ? sfk::kAffine16HC : sfk::kAffine16C)
+                                            : sfk::kAffineC;
+    const int nc = key.kind == PK_AFFINE16 ? (half ? sfk::kAffine16HNC : sfk::kAffine16NC)
+                                           : sfk::kAffineNC;
     for (int q = 0; q < nc; ++q)
-      if (cs[q] > key.c && (int)out.size() < 3) out.push_back(ClassChoice{cs[q], 32});
+      if (cs[q] > key.c && (int)out.size() < 3) out.push_back(ClassChoice{cs[q], key.lanes});
+    // 16-bit rows: the other lane count per pass (two passes per warp, or one), its two
+    // narrowest classes that hold the group's widest row (`blocks` carries it here).
+    const int other = half ? 32 : 16;
+    const int* os = half ? sfk::kAffine16C : sfk::kAffine16HC;
+    const int no = half ? sfk::kAffine16NC : sfk::kAffine16HNC;
+    int added = 0;
+    if (key.kind == PK_AFFINE16)
+      for (int q = 0; q < no && added < 2; ++q)
+        if ((int64_t)other * os[q] >= blocks) {
+          out.push_back(ClassChoice{os[q], other});
+          ++added;
+        }
   }
   return out;
 }

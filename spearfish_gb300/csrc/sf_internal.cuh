@@ -160,6 +160,11 @@ cudaError_t launch_affine16(int c, bool tb, const AffLaunch& a, int grid, int bl
                             cudaStream_t s);
 extern const int kAffine16C[];
 extern const int kAffine16NC;
+// The same rows with 16 lanes to a pass, two passes per warp.
+cudaError_t launch_affine16h(int c, bool tb, const AffLaunch& a, int grid, int block,
+                             cudaStream_t s);
+extern const int kAffine16HC[];
+extern const int kAffine16HNC;
 
 
 struct MyersLaunch {

@@ -28,7 +28,8 @@ struct Pos {
 struct TbLayout {
   int32_t C, C2, TG;
   bool wide, p16;
-  uint32_t row;  // word pairs per row
+  int32_t lanes;  // lanes of a pass: 32, or 16 for the half-warp 16-bit rows
+  uint32_t row;   // word pairs per row
 
   __device__ __forceinline__ Pos at(int32_t K) const {
     Pos p;
@@ -60,7 +61,7 @@ struct TbLayout {
       const int hi = p.c >= C2, k = hi ? p.c - C2 : p.c;
       const int g = k >> 3, t = k & 7;
       sh = 8 * hi + t;
-      return g * 32 + p.L;
+      return g * lanes + p.L;
     }
     const int g = p.c >> 4, q = p.c & 15;
     const int gs = (C - 16 * g) < 16 ? (C - 16 * g) : 16;
@@ -85,15 +86,17 @@ struct TbLayout {
 
 
 template <int C>
-__device__ __forceinline__ TbLayout tb_layout(bool wide, bool p16, const DJob& J, uint32_t flags) {
+__device__ __forceinline__ TbLayout tb_layout(bool wide, bool p16, const DJob& J, uint32_t flags,
+                                              int lanes = 32) {
   TbLayout Y;
   Y.C = C;
   Y.C2 = C / 2;
   Y.TG = (C + 15) / 16;
   Y.wide = wide;
   Y.p16 = p16;
+  Y.lanes = lanes;
   const int64_t chunks = wide ? wide_chunks(C, band_wmax(J, flags)) : 1;
-  Y.row = (uint32_t)(tb_row_words(C, chunks) / 2);
+  Y.row = (uint32_t)(tb_row_words(C, chunks) / 2 * lanes / 32);
   return Y;
 }
 

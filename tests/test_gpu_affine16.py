@@ -53,10 +53,13 @@ class Jobs:
                 jobs[q][k] = v
         return jobs
 
-    def run(self, ctx, scores, int16=True):
-        """Runs the jobs in one plan; returns the output and the bucket kinds it used."""
+    def run(self, ctx, scores, int16=True, lanes=32):
+        """Runs the jobs in one plan (16-bit passes on `lanes` lanes each where they fit);
+        returns the output and the bucket kinds it used."""
         old = os.environ.get("SF_AFFINE16")
+        old_l = os.environ.get("SF_AFFINE16_LANES")
         os.environ["SF_AFFINE16"] = "1" if int16 else "0"
+        os.environ["SF_AFFINE16_LANES"] = str(lanes)
         try:
             pool = self.pool.build()
             jobs = self.jobs()
@@ -65,14 +68,16 @@ class Jobs:
                 plan.upload(pool)
                 plan.execute()
                 out = plan.download()
-                kinds = {(b["kind"], b["c"]) for b in json.loads(plan.describe())["buckets"]}
+                kinds = {(b["kind"], b["c"]) if b["lanes"] == 32 or b["kind"] != "affine16"
+                         else ("affine16h", b["c"]) for b in json.loads(plan.describe())["buckets"]}
             finally:
                 plan.close()
         finally:
-            if old is None:
-                del os.environ["SF_AFFINE16"]
-            else:
-                os.environ["SF_AFFINE16"] = old
+            for k, v in (("SF_AFFINE16", old), ("SF_AFFINE16_LANES", old_l)):
+                if v is None:
+                    del os.environ[k]
+                else:
+                    os.environ[k] = v
         return out, kinds
 
 
@@ -205,3 +210,33 @@ def test_sorted_cut_bookkeeping(ctx):
                 got = gpu.affine_extend_sorted_cut_bonus(p, texts, sc, band, *args)
                 want = O.affine_extend_sorted_cut_bonus(p, texts, sc, band, *args)
                 assert got == want, args
+
+
+def test_half_warp_passes(ctx):
+    """Two passes per warp (16 lanes each): every half-warp class, passes of uneven lengths
+    paired in one warp, Global and Prefix with CIGARs, X-drop and bonuses -- identical to the
+    one-pass-per-warp kernel and to the oracle."""
+    rng = np.random.default_rng(1605)
+    J = Jobs()
+    for band in (2, 30, 55, 70, 90, 110, 120, 130, 150, 170):
+        for rep in range(4):
+            m = int(rng.integers(max(20, 2 * band), 2 * band + 1500))
+            p, t = R.rand_pair(m, int(rng.integers(3, 15)), int(rng.integers(1, 2 ** 62)))
+            mode = R.GLOBAL if rep % 2 == 0 else R.PREFIX
+            sci = int(rng.integers(0, 2))
+            J.add(None, p=p, t=t, kind=1, mode=mode, band=band, want_cigar=rep % 3 != 2,
+                  sc_index=sci)
+            w = len(t) + int(rng.integers(0, 100))
+            xd = int(rng.integers(10, 200)) if rng.random() < 0.7 else R.I32_MAX
+            J.add(None, p=p, t=t, kind=2, band=band, window=w, xdrop=xd,
+                  end_bonus=int(rng.integers(0, 9)), want_cigar=rep % 2, sc_index=sci)
+    for m in (0, 1, 5):  # short and empty patterns among long ones
+        p, t = R.rand_pair(m, 5, int(rng.integers(1, 2 ** 62)))
+        J.add(None, p=p, t=t, kind=1, mode=R.GLOBAL, band=40, want_cigar=1)
+    scores = (R.ONT, R.HIFI)
+    out, kinds = J.run(ctx, scores, lanes=16)
+    half = {c for k, c in kinds if k == "affine16h"}
+    assert half >= {8, 10, 12, 16, 20, 24}, sorted(half)
+    _check(J, out, scores)
+    out32, _ = J.run(ctx, scores, lanes=32)
+    _same(out, out32)
