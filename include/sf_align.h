@@ -214,8 +214,9 @@ typedef struct {
     uint8_t mode;   /* sf_mode (Myers, affine) */
     uint8_t want_cigar;
     uint8_t text_src; /* SF_TEXT_POOL: t_off is a byte offset in the pool;
-                         SF_TEXT_STORE: t_off is a base position in the context's
-                         transcript store (sf_context_use_store) */
+                         SF_TEXT_STORE(_REV): t_off is a base position in the
+                         context's transcript store (sf_context_use_store), the
+                         window read forwards (backwards) */
     uint32_t k;      /* Myers threshold (SF_NONE: none) */
     uint64_t band;   /* affine band (SF_NOLIMIT: none) */
     uint64_t window; /* extend window */
@@ -301,7 +302,12 @@ int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
  * store's concatenation, as `tx_range` numbers it; n = its length): the window
  * is sliced on the device, so a batch uploads only reads and descriptors.  The
  * store must outlive every plan execution that reads it. */
-enum { SF_TEXT_POOL = 0, SF_TEXT_STORE = 1 };
+enum {
+    SF_TEXT_POOL = 0,
+    SF_TEXT_STORE = 1,
+    SF_TEXT_STORE_REV = 2 /* the store window read backwards (a leftward extension's
+                             flank, as the mapper reverses it: lib.rs:2024-2027) */
+};
 typedef struct sf_store sf_store;
 
 /* A store of `count` transcripts given as byte codes (0..3), concatenated in
@@ -353,6 +359,37 @@ typedef struct {
 int sf_banded_batch(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                     const sf_banded_read_t *reads, uint64_t n_reads,
                     const sf_span_t *texts, uint64_t n_texts, uint32_t *out);
+
+/* lib.rs:414-425 `Ends`: the span-end extensions' scoring, band, end bonus,
+ * X-drop, and the transcript flank searched beyond the read flank's length,
+ * pad + flank / pad_div. */
+typedef struct {
+    sf_affine_t sc;
+    uint64_t band;
+    int32_t end_bonus, xdrop;
+    uint32_t pad, pad_div;
+} sf_ends_t;
+
+/* A hit whose span is extended over the read's flanks (the TxHit fields
+ * `extend_ends` reads and writes): the read in the hit's orientation (codes
+ * in the pool), its transcript (a range of the context's store) and the span's
+ * read / transcript coordinates, updated in place. */
+typedef struct {
+    uint64_t read_off;   /* the read's codes in the pool */
+    uint64_t tx_start;   /* the transcript's first base in the store */
+    uint32_t read_len, tx_len;
+    uint32_t qstart, qend, tstart, tend;
+} sf_hit_t;
+
+/* lib.rs:2020-2035 `extend_ends` (with 2046-2073 `right_reach` and 2100-2114
+ * `extend_dp`) for n hits in one device batch: each span extended leftwards
+ * over the read prefix and the transcript flank before it (both read
+ * backwards, lib.rs:2024-2027) when qstart > 0 and tstart > 0, and rightwards
+ * when the read and the transcript go on.  The flanks are read from the
+ * context's store; the reference's per-read cache of extensions
+ * (lib.rs:427-430) only avoids recomputing equal results. */
+int sf_extend_ends_batch(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
+                         const sf_ends_t *e, sf_hit_t *hits, uint64_t n);
 
 /* ---- serving: continuous batching ---------------------------------------
  * Requests (the jobs of a read batch over a byte pool the caller keeps alive

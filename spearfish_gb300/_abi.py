@@ -62,6 +62,17 @@ class BandedReadT(C.Structure):
                 ("distinct", C.c_uint32), ("pad_", C.c_uint32)]
 
 
+class EndsT(C.Structure):
+    _fields_ = [("sc", Affine), ("band", C.c_uint64), ("end_bonus", C.c_int32),
+                ("xdrop", C.c_int32), ("pad", C.c_uint32), ("pad_div", C.c_uint32)]
+
+
+class HitT(C.Structure):
+    _fields_ = [("read_off", C.c_uint64), ("tx_start", C.c_uint64), ("read_len", C.c_uint32),
+                ("tx_len", C.c_uint32), ("qstart", C.c_uint32), ("qend", C.c_uint32),
+                ("tstart", C.c_uint32), ("tend", C.c_uint32)]
+
+
 class ResultT(C.Structure):
     _fields_ = [("score", C.c_int32), ("distance", C.c_uint32), ("pattern_end", C.c_uint64),
                 ("text_start", C.c_uint64), ("text_end", C.c_uint64), ("text_read", C.c_uint64),
@@ -107,6 +118,8 @@ SIGNATURES = {
     "sf_store_destroy": (None, [_vp]),
     "sf_store_bases": (C.c_uint64, [_vp]),
     "sf_context_use_store": (C.c_int, [_vp, _vp]),
+    "sf_extend_ends_batch": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(EndsT), C.POINTER(HitT),
+                                       C.c_uint64]),
     "sf_banded": (C.c_int, [_u8p, C.c_uint64, _u8pp, _u64p, C.c_uint64, C.c_int, C.c_uint32,
                             C.c_int, _u32p]),
     "sf_banded_batch": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(BandedReadT), C.c_uint64,

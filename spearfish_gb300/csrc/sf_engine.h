@@ -194,6 +194,10 @@ struct sf_store {
 constexpr uint64_t kStorePad = 16;
 // Pass::t_off of a store window: the flag plus the window's first position in the store.
 constexpr uint64_t kStoreFlag = uint64_t(1) << 63;
+// Pass::p_off / t_off read backwards (byte pool or store), as the mapper's leftward
+// extensions read their read prefix and transcript flank.
+constexpr uint64_t kRevFlag = uint64_t(1) << 62;
+constexpr uint64_t kOffMask = ~(kStoreFlag | kRevFlag);
 
 struct sf_context {
   int dev = 0;

@@ -205,8 +205,8 @@ int plan_build(sf_plan* P) {
   keys.reserve(2 * np);
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
-    if (p.p_off + p.m > P->pool_bytes ||
-        (!(p.t_off & kStoreFlag) && p.t_off + p.n > P->pool_bytes))
+    if ((p.p_off & kOffMask) + p.m > P->pool_bytes ||
+        (!(p.t_off & kStoreFlag) && (p.t_off & kOffMask) + p.n > P->pool_bytes))
       return fail(SF_ERR_INVALID, "job sequence outside the pool");
     if ((p.t_off & kStoreFlag) && !ctx->store)
       return fail(SF_ERR_INVALID, "store text but the context uses no store");
@@ -287,7 +287,7 @@ int plan_build(sf_plan* P) {
     DJob j = make_djob(p, flags);
     j.p_word = word_of[2 * q];
     j.t_word = word_of[2 * q + 1];
-    j.p_byte = p.p_off;
+    j.p_byte = p.p_off & kOffMask;
     const int64_t wmax = band_wmax(j, flags);
     int c = 4;
     bool wide = false;
@@ -825,14 +825,15 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
     p.m = j.m;
     p.n = j.n;
     if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
-    if (j.text_src > SF_TEXT_STORE) return fail(SF_ERR_INVALID, "bad text source");
+    if (j.text_src > SF_TEXT_STORE_REV) return fail(SF_ERR_INVALID, "bad text source");
     if (j.p_off > pool_bytes || j.m > pool_bytes - j.p_off)
       return fail(SF_ERR_INVALID, "job sequence outside the pool");
-    if (j.text_src == SF_TEXT_STORE) {
+    if (j.text_src == SF_TEXT_STORE || j.text_src == SF_TEXT_STORE_REV) {
       if (!store) return fail(SF_ERR_INVALID, "store text but the context uses no store");
       if (j.t_off > store->bases || j.n > store->bases - j.t_off)
         return fail(SF_ERR_INVALID, "text window outside the store");
-      p.t_off = kStoreFlag | (j.t_off + kStorePad);
+      p.t_off = kStoreFlag | (j.text_src == SF_TEXT_STORE_REV ? kRevFlag : 0) |
+                (j.t_off + kStorePad);
     } else if (j.t_off > pool_bytes || j.n > pool_bytes - j.t_off) {
       return fail(SF_ERR_INVALID, "job sequence outside the pool");
     }
@@ -1536,6 +1537,93 @@ int sf_banded_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
   for (uint64_t r = 0; r < n_reads; ++r)
     banded_finish(reads[r].count, first_of[r], is_first[r], dist.data() + reads[r].first,
                   reads[r].cap, out + reads[r].first);
+  return SF_OK;
+}
+
+// ---- span-end extensions (map/src/lib.rs:2020-2114 `extend_ends`, `right_reach`) -------
+
+int sf_extend_ends_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
+                         const sf_ends_t* e, sf_hit_t* hits, uint64_t n) {
+  if (!ctx || !e || (n && !hits) || (pool_bytes && !pool)) return fail(SF_ERR_INVALID, "bad argument");
+  if (!ctx->store) return fail(SF_ERR_INVALID, "extensions read their flanks from the store");
+  if (e->pad_div == 0 || !ok_sc(&e->sc)) return fail(SF_ERR_INVALID, "bad extension parameters");
+  const sf_store* store = ctx->store;
+  // lib.rs:2021: the transcript flank searched: the read flank plus pad + flank / pad_div.
+  auto window = [&](uint32_t x) { return (uint64_t)x + e->pad + x / e->pad_div; };
+  std::vector<Pass> ps;
+  std::vector<std::pair<uint64_t, int>> slot;  // (hit, 0 left / 1 right) per pass
+  for (uint64_t q = 0; q < n; ++q) {
+    const sf_hit_t& h = hits[q];
+    if (h.read_off > pool_bytes || h.read_len > pool_bytes - h.read_off)
+      return fail(SF_ERR_INVALID, "read outside the pool");
+    if (h.tx_start > store->bases || h.tx_len > store->bases - h.tx_start)
+      return fail(SF_ERR_INVALID, "transcript outside the store");
+    if (h.qstart > h.qend || h.qend > h.read_len || h.tstart > h.tend || h.tend > h.tx_len)
+      return fail(SF_ERR_INVALID, "bad hit span");
+    Pass p;
+    p.kind = PK_AFFINE;
+    p.mode = SF_PREFIX;
+    p.band = e->band;
+    p.clip = true;
+    p.cell = true;
+    p.xdrop = e->xdrop;
+    p.end_bonus = e->end_bonus;
+    p.tb_kind = 1;
+    p.sc = e->sc;
+    if (h.qstart > 0 && h.tstart > 0) {
+      // lib.rs:2022-2031: the read prefix and the transcript flank before tstart, backwards.
+      const uint64_t w = window(h.qstart);
+      const uint64_t lo = h.tstart > w ? h.tstart - w : 0;
+      Pass L = p;
+      L.p_off = kRevFlag | h.read_off;
+      L.m = h.qstart;
+      L.t_off = kStoreFlag | kRevFlag | (h.tx_start + lo + kStorePad);
+      L.n = (uint32_t)(h.tstart - lo);
+      L.geom = std::max<uint64_t>(w, L.n);
+      ps.push_back(L);
+      slot.push_back({q, 0});
+    }
+    const uint32_t rest = h.read_len - h.qend;
+    if (rest > 0 && h.tend < h.tx_len) {
+      // lib.rs:2046-2073: the read suffix and the flank after tend, cut at the transcript's end.
+      const uint64_t w = window(rest);
+      const uint64_t hi = std::min<uint64_t>(h.tend + w, h.tx_len);
+      Pass R = p;
+      R.p_off = h.read_off + h.qend;
+      R.m = rest;
+      R.t_off = kStoreFlag | (h.tx_start + h.tend + kStorePad);
+      R.n = (uint32_t)(hi - h.tend);
+      R.geom = std::max<uint64_t>(w, R.n);
+      ps.push_back(R);
+      slot.push_back({q, 1});
+    }
+  }
+  if (ps.empty()) return SF_OK;
+  if (!ctx->cache) {
+    ctx->cache.reset(new sf_plan);
+    ctx->cache->ctx = ctx;
+  }
+  sf_plan* P = ctx->cache.get();
+  P->passes = std::move(ps);
+  P->pool_bytes = pool_bytes;
+  int rc;
+  if ((rc = plan_build(P))) return rc;
+  if ((rc = plan_upload_from(P, pool))) return rc;
+  if ((rc = plan_execute(P, false))) return rc;
+  if ((rc = plan_fetch(P))) return rc;
+  std::vector<sf_result_t> res(P->passes.size());
+  if ((rc = plan_results(P, res.data(), nullptr, 0, 0, false))) return rc;
+  // lib.rs:2029-2032 (left: the span starts qi / tj bases earlier) and 2072 (right).
+  for (size_t u = 0; u < res.size(); ++u) {
+    sf_hit_t& h = hits[slot[u].first];
+    if (slot[u].second == 0) {
+      h.qstart -= (uint32_t)res[u].pattern_end;
+      h.tstart -= (uint32_t)res[u].text_end;
+    } else {
+      h.qend += (uint32_t)res[u].pattern_end;
+      h.tend += (uint32_t)res[u].text_end;
+    }
+  }
   return SF_OK;
 }
 

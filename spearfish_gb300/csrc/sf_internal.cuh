@@ -182,7 +182,8 @@ extern const int kMyersB[];
 extern const int kMyersNB;
 
 // Sequences of a batch into its packed pool: from the byte pool, or (byte_off with bit 63
-// set) sliced from the transcript store's packed words at that base position.
+// set) sliced from the transcript store's packed words at that base position; bit 62 reads
+// the sequence backwards.
 struct PackLaunch {
   const uint8_t* bytes;
   const uint64_t* byte_off;  // per sequence

@@ -15,27 +15,46 @@ __global__ void __launch_bounds__(256) pack_kernel(sfk::PackLaunch a) {
     const uint64_t len = a.len[s];
     const uint64_t words = (len + 1 + 15) / 16;  // one leading pad base
     uint32_t* dst = a.pool + a.word_off[s];
+    const bool rev = (off >> 62) & 1;  // read backwards (the mapper's leftward extensions)
     if (off >> 63) {
-      // A window of the transcript store: packed base x (x >= 1) is store position
-      // pos + x - 1; the pad base takes the store base before the window (never matched).
-      const uint64_t pos = (off & ~(uint64_t(1) << 63)) - 1;
-      for (uint64_t w = lane; w < words; w += 32) {
-        const uint64_t b0 = pos + 16 * w, wi = b0 >> 4;
-        uint32_t v = __funnelshift_r(__ldg(a.store + wi), __ldg(a.store + wi + 1),
-                                     2u * (uint32_t)(b0 & 15));
-        const uint64_t valid = len + 1 - 16 * w;  // bases of this word inside the window
-        if (valid < 16) v &= (1u << (2 * valid)) - 1u;
-        dst[w] = v;
+      const uint64_t pos = (off & ~(uint64_t(3) << 62)) - 1;
+      if (!rev) {
+        // A window of the transcript store: packed base x (x >= 1) is store position
+        // pos + x - 1; the pad base takes the store base before the window (never matched).
+        for (uint64_t w = lane; w < words; w += 32) {
+          const uint64_t b0 = pos + 16 * w, wi = b0 >> 4;
+          uint32_t v = __funnelshift_r(__ldg(a.store + wi), __ldg(a.store + wi + 1),
+                                       2u * (uint32_t)(b0 & 15));
+          const uint64_t valid = len + 1 - 16 * w;  // bases of this word inside the window
+          if (valid < 16) v &= (1u << (2 * valid)) - 1u;
+          dst[w] = v;
+        }
+      } else {
+        // The window read backwards: packed base x (1 <= x <= len) is store position
+        // pos + len - x + 1.
+        for (uint64_t w = lane; w < words; w += 32) {
+          uint32_t v = 0;
+#pragma unroll
+          for (int b = 0; b < 16; ++b) {
+            const uint64_t x = 16 * w + b;
+            if (x >= 1 && x <= len) {
+              const uint64_t sp = pos + len - x + 1;
+              v |= ((__ldg(a.store + (sp >> 4)) >> (2 * (sp & 15))) & 3u) << (2 * b);
+            }
+          }
+          dst[w] = v;
+        }
       }
       continue;
     }
-    const uint8_t* src = a.bytes + off;
+    const uint8_t* src = a.bytes + (off & ~(uint64_t(3) << 62));
     for (uint64_t w = lane; w < words; w += 32) {
       uint32_t v = 0;
 #pragma unroll
       for (int b = 0; b < 16; ++b) {
         const uint64_t pos = 16 * w + b;
-        if (pos >= 1 && pos - 1 < len) v |= (uint32_t)(src[pos - 1] & 3) << (2 * b);
+        if (pos >= 1 && pos - 1 < len)
+          v |= (uint32_t)(src[rev ? len - pos : pos - 1] & 3) << (2 * b);
       }
       dst[w] = v;
     }

@@ -60,3 +60,25 @@ def banded_batch(ctx: Context, reads: Sequence) -> list[list[int]]:
         res.append([int(v) for v in out[at:at + len(texts)]])
         at += len(texts)
     return res
+
+
+def extend_ends_batch(ctx: Context, pool: np.ndarray, ends: dict, hits: np.ndarray) -> np.ndarray:
+    """lib.rs:2020-2114 `extend_ends` for many hits in one device batch (texts from the
+    context's transcript store).  `ends`: sc (mat, mis, open, ext), band, end_bonus, xdrop,
+    pad, pad_div.  `hits`: a HIT_DTYPE array (read_off, tx_start, read_len, tx_len, qstart,
+    qend, tstart, tend); returns a copy with the spans extended."""
+    from .align import _aff
+    out = np.ascontiguousarray(hits, dtype=HIT_DTYPE).copy()
+    pool = np.ascontiguousarray(pool, dtype=np.uint8)
+    e = _abi.EndsT(_aff(ends["sc"]), int(ends["band"]), int(ends["end_bonus"]), int(ends["xdrop"]),
+                   int(ends["pad"]), int(ends["pad_div"]))
+    _abi.check(_abi.load().sf_extend_ends_batch(
+        ctx.handle, pool.ctypes.data_as(C.POINTER(C.c_uint8)), pool.size, C.byref(e),
+        out.ctypes.data_as(C.POINTER(_abi.HitT)), len(out)))
+    return out
+
+
+HIT_DTYPE = np.dtype([("read_off", "<u8"), ("tx_start", "<u8"), ("read_len", "<u4"),
+                      ("tx_len", "<u4"), ("qstart", "<u4"), ("qend", "<u4"), ("tstart", "<u4"),
+                      ("tend", "<u4")], align=True)
+assert HIT_DTYPE.itemsize == C.sizeof(_abi.HitT)

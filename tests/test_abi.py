@@ -44,6 +44,8 @@ def test_struct_layouts(lib):
     assert C.sizeof(_abi.CigarT) == 40
     assert C.sizeof(_abi.SpanT) == 16
     assert C.sizeof(_abi.BandedReadT) == 40
+    assert C.sizeof(_abi.EndsT) == 40
+    assert C.sizeof(_abi.HitT) == 40
     assert batch.JOB_DTYPE.itemsize == 80 and batch.RESULT_DTYPE.itemsize == 64
 
 

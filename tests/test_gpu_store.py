@@ -111,3 +111,38 @@ def test_store_windows_equal_pool_texts():
         else:
             o = O.traceback(read, win, O.TB_EXTEND, O.PREFIX, R.ONT, 16, rows[q]["window"], 5, 50)
             assert (int(r["score"]), got.cigar(q)) == (o["score"], o["cigar"])
+
+
+def test_store_windows_read_backwards():
+    """SF_TEXT_STORE_REV: a window read backwards equals its reversed codes in the pool."""
+    from spearfish_gb300 import build
+    build.build()
+    from spearfish_gb300 import batch as B
+    rng = np.random.default_rng(1902)
+    txs = [rng.integers(0, 4, int(rng.integers(100, 3000)), dtype=np.uint8) for _ in range(30)]
+    starts = np.concatenate([[0], np.cumsum([t.size for t in txs])[:-1]]).astype(np.uint64)
+    pb = B.PoolBuilder()
+    rows, copies = [], []
+    for q in range(150):
+        x = int(rng.integers(0, len(txs)))
+        t = txs[x]
+        a = int(rng.integers(0, t.size))
+        b = int(rng.integers(a, t.size + 1))
+        win = t[a:b][::-1]
+        read = R.mutate(win.tolist(), R.rand_edits(rng, max(1, len(win) // 10), max(1, len(win))))
+        f = {"p_off": pb.add(read), "m": len(read), "n": int(win.size),
+             "kind": 2 if q % 2 else 0, "band": 16, "window": int(win.size) + 20, "xdrop": 50,
+             "end_bonus": 5, "mode": R.INFIX if q % 2 == 0 else 1}
+        copies.append(dict(f, t_off=pb.add(win), text_src=B.TEXT_POOL))
+        rows.append(dict(f, t_off=int(starts[x]) + a, text_src=2))
+    pool = pb.build()
+    ctx = B.Context(0)
+    store = B.Store(ctx, txs)
+    try:
+        ref = B.run(ctx, pool, _jobs(B, copies))
+        ctx.use_store(store)
+        _same(ref, B.run(ctx, pool, _jobs(B, rows)))
+    finally:
+        ctx.use_store(None)
+        store.close()
+        ctx.close()
