@@ -391,6 +391,35 @@ typedef struct {
 int sf_extend_ends_batch(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                          const sf_ends_t *e, sf_hit_t *hits, uint64_t n);
 
+/* The tie-break's sorted DP calls (lib.rs:1294-1884 `segmented`: a read
+ * segment against the candidates' distinct texts in sorted order) for many
+ * segments in one batch.  Each call is one of the two sorted entry points. */
+enum {
+    SF_SORTED_AFFINE = 0,    /* align.rs:854-861 `affine_sorted` in `mode` */
+    SF_SORTED_EXTEND_CUT = 1 /* align.rs:903-949 `affine_extend_sorted_cut_bonus` */
+};
+typedef struct {
+    uint64_t p_off;    /* the read segment's codes in the pool */
+    uint64_t first;    /* its first text in the text list */
+    uint64_t band;
+    uint64_t window;   /* extend: the window the band is laid out for */
+    uint64_t cut;      /* extend: the cut (SF_NOLIMIT: none) */
+    uint32_t m, count; /* segment length; texts [first, first + count) */
+    uint32_t kind;     /* SF_SORTED_* */
+    uint32_t mode;     /* affine_sorted's mode */
+    int32_t end_bonus, xdrop;
+    uint32_t diagonal, track_cut, bonus_within_cut;
+    uint32_t sc_index; /* into `scores` */
+} sf_sorted_call_t;
+
+/* out[q] for texts[q]: the entry point's (whole, cut, cols) triple; for
+ * affine_sorted the score as (x, x, 0), as lib.rs:1442-1445 uses it.  Equal to
+ * the one-call entry points text by text. */
+int sf_sorted_batch(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
+                    const sf_affine_t *scores, uint32_t n_scores,
+                    const sf_sorted_call_t *calls, uint64_t n_calls,
+                    const sf_span_t *texts, uint64_t n_texts, sf_cut_t *out);
+
 /* ---- serving: continuous batching ---------------------------------------
  * Requests (the jobs of a read batch over a byte pool the caller keeps alive
  * until it waits for them) are admitted in arrival order as soon as a slot

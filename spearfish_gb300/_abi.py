@@ -73,6 +73,15 @@ class HitT(C.Structure):
                 ("tstart", C.c_uint32), ("tend", C.c_uint32)]
 
 
+class SortedCallT(C.Structure):
+    _fields_ = [("p_off", C.c_uint64), ("first", C.c_uint64), ("band", C.c_uint64),
+                ("window", C.c_uint64), ("cut", C.c_uint64), ("m", C.c_uint32),
+                ("count", C.c_uint32), ("kind", C.c_uint32), ("mode", C.c_uint32),
+                ("end_bonus", C.c_int32), ("xdrop", C.c_int32), ("diagonal", C.c_uint32),
+                ("track_cut", C.c_uint32), ("bonus_within_cut", C.c_uint32),
+                ("sc_index", C.c_uint32)]
+
+
 class ResultT(C.Structure):
     _fields_ = [("score", C.c_int32), ("distance", C.c_uint32), ("pattern_end", C.c_uint64),
                 ("text_start", C.c_uint64), ("text_end", C.c_uint64), ("text_read", C.c_uint64),
@@ -120,6 +129,8 @@ SIGNATURES = {
     "sf_context_use_store": (C.c_int, [_vp, _vp]),
     "sf_extend_ends_batch": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(EndsT), C.POINTER(HitT),
                                        C.c_uint64]),
+    "sf_sorted_batch": (C.c_int, [_vp, _u8p, C.c_uint64, _aff, C.c_uint32, C.POINTER(SortedCallT),
+                                  C.c_uint64, C.POINTER(SpanT), C.c_uint64, C.POINTER(CutT)]),
     "sf_banded": (C.c_int, [_u8p, C.c_uint64, _u8pp, _u64p, C.c_uint64, C.c_int, C.c_uint32,
                             C.c_int, _u32p]),
     "sf_banded_batch": (C.c_int, [_vp, _u8p, C.c_uint64, C.POINTER(BandedReadT), C.c_uint64,

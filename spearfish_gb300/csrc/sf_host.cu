@@ -1627,6 +1627,87 @@ int sf_extend_ends_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_byt
   return SF_OK;
 }
 
+// ---- sorted calls in a batch (the DP of map/src/lib.rs:1294-1884 `segmented`) ---------
+
+int sf_sorted_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
+                    const sf_affine_t* scores, uint32_t n_scores, const sf_sorted_call_t* calls,
+                    uint64_t n_calls, const sf_span_t* texts, uint64_t n_texts, sf_cut_t* out) {
+  if (!ctx || (n_calls && !calls) || (n_texts && (!texts || !out)) || (pool_bytes && !pool) ||
+      (n_scores && !scores))
+    return fail(SF_ERR_INVALID, "bad argument");
+  std::vector<Pass> ps;
+  std::vector<uint64_t> text_of;
+  for (uint64_t c = 0; c < n_calls; ++c) {
+    const sf_sorted_call_t& k = calls[c];
+    if (k.sc_index >= n_scores || !ok_sc(&scores[k.sc_index]))
+      return fail(SF_ERR_INVALID, "bad scoring index");
+    if (k.kind > SF_SORTED_EXTEND_CUT) return fail(SF_ERR_INVALID, "bad sorted call kind");
+    if (k.kind == SF_SORTED_AFFINE && !ok_mode((int)k.mode)) return fail(SF_ERR_INVALID, "bad mode");
+    if (k.first > n_texts || k.count > n_texts - k.first)
+      return fail(SF_ERR_INVALID, "call's texts outside the text list");
+    if (k.p_off > pool_bytes || k.m > pool_bytes - k.p_off)
+      return fail(SF_ERR_INVALID, "pattern outside the pool");
+    if (k.m >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+    const sf_affine_t* sc = &scores[k.sc_index];
+    for (uint64_t q = 0; q < k.count; ++q) {
+      const sf_span_t& t = texts[k.first + q];
+      if (t.off > pool_bytes || t.len > pool_bytes - t.off)
+        return fail(SF_ERR_INVALID, "text outside the pool");
+      if (t.len >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+      if (k.kind == SF_SORTED_AFFINE) {
+        // align.rs:854-861 `affine_sorted`: one Global/Prefix/Infix pass per text.
+        ps.push_back(affine_pass(k.p_off, k.m, t.off, t.len, (int)k.mode, sc, k.band));
+      } else {
+        // align.rs:903-949 `affine_extend_sorted_cut_bonus` (the passes of 917-928).
+        Pass p = affine_pass(k.p_off, k.m, t.off, t.len, SF_PREFIX, sc, k.band);
+        p.geom = k.diagonal ? std::min<uint64_t>(k.m, t.len) : std::max<uint64_t>(t.len, k.window);
+        p.clip = true;
+        p.xdrop = k.xdrop;
+        p.cell = k.track_cut && k.cut != SF_NOLIMIT;
+        p.cut = k.cut;
+        ps.push_back(p);
+      }
+      text_of.push_back(k.first + q);
+    }
+  }
+  if (ps.empty()) return SF_OK;
+  if (!ctx->cache) {
+    ctx->cache.reset(new sf_plan);
+    ctx->cache->ctx = ctx;
+  }
+  sf_plan* P = ctx->cache.get();
+  P->passes = std::move(ps);
+  P->pool_bytes = pool_bytes;
+  int rc;
+  if ((rc = plan_build(P))) return rc;
+  if ((rc = plan_upload_from(P, pool))) return rc;
+  if ((rc = plan_execute(P, false))) return rc;
+  if ((rc = plan_fetch(P))) return rc;
+  const DRes* rs = P->h_res.as<DRes>();
+  size_t u = 0;
+  for (uint64_t c = 0; c < n_calls; ++c) {
+    const sf_sorted_call_t& k = calls[c];
+    for (uint64_t q = 0; q < k.count; ++q, ++u) {
+      const DRes& d = rs[P->slot[u]];
+      sf_cut_t& o = out[text_of[u]];
+      if (k.kind == SF_SORTED_AFFINE) {
+        // lib.rs:1442-1445: an affine_sorted score stands for whole and cut, no columns.
+        o.whole = o.cut = d.score;
+        o.cols = 0;
+        continue;
+      }
+      // align.rs:929-948
+      const int32_t end = (k.bonus_within_cut && k.cut != SF_NOLIMIT)
+                              ? std::max(d.score, sat_add32(d.cut_score, k.end_bonus))
+                              : sat_add32(d.score, k.end_bonus);
+      o.whole = std::max(d.clip_best, end);
+      o.cols = d.clip_best >= end ? d.clip_j : d.score_col;
+      o.cut = k.cut == SF_NOLIMIT ? o.whole : std::max(d.cut_best, sat_add32(d.cut_score, k.end_bonus));
+    }
+  }
+  return SF_OK;
+}
+
 int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, const sf_job_t* jobs,
                  uint64_t count, const sf_affine_t* scores, uint32_t n_scores,
                  sf_result_t* results, uint32_t* ops, uint64_t ops_cap, uint64_t* ops_used) {

@@ -82,3 +82,50 @@ HIT_DTYPE = np.dtype([("read_off", "<u8"), ("tx_start", "<u8"), ("read_len", "<u
                       ("tx_len", "<u4"), ("qstart", "<u4"), ("qend", "<u4"), ("tstart", "<u4"),
                       ("tend", "<u4")], align=True)
 assert HIT_DTYPE.itemsize == C.sizeof(_abi.HitT)
+
+
+SORTED_AFFINE, SORTED_EXTEND_CUT = 0, 1
+
+
+def sorted_batch(ctx: Context, calls: Sequence, scores: Sequence = ((2, 4, 4, 2),)) -> list:
+    """The tie-break's sorted DP calls for many read segments in one batch (sf_sorted_batch).
+    Each call: dict(read, texts, kind, band, and for SORTED_AFFINE mode; for
+    SORTED_EXTEND_CUT end_bonus, xdrop, diagonal, window, cut (None: none), track_cut,
+    bonus_within_cut; sc_index).  Returns per call the list of (whole, cut, cols)."""
+    from .align import _aff
+    pb = PoolBuilder()
+    cs = (_abi.SortedCallT * max(1, len(calls)))()
+    spans = []
+    for i, k in enumerate(calls):
+        c = cs[i]
+        c.p_off = pb.add(k["read"])
+        c.m = len(k["read"])
+        c.first = len(spans)
+        c.count = len(k["texts"])
+        c.kind = int(k["kind"])
+        c.mode = int(k.get("mode", 2))
+        c.band = _abi.SF_NOLIMIT if k["band"] is None else int(k["band"])
+        c.window = int(k.get("window", 0))
+        cut = k.get("cut")
+        c.cut = _abi.SF_NOLIMIT if cut is None else int(cut)
+        c.end_bonus = int(k.get("end_bonus", 0))
+        c.xdrop = int(k.get("xdrop", 2 ** 31 - 1))
+        c.diagonal = int(bool(k.get("diagonal", False)))
+        c.track_cut = int(bool(k.get("track_cut", True)))
+        c.bonus_within_cut = int(bool(k.get("bonus_within_cut", False)))
+        c.sc_index = int(k.get("sc_index", 0))
+        for t in k["texts"]:
+            spans.append((pb.add(t), len(t)))
+    pool = pb.build()
+    sp = (_abi.SpanT * max(1, len(spans)))(*[_abi.SpanT(o, n) for o, n in spans])
+    sc = (_abi.Affine * max(1, len(scores)))(*[_aff(s) for s in scores])
+    out = (_abi.CutT * max(1, len(spans)))()
+    _abi.check(_abi.load().sf_sorted_batch(
+        ctx.handle, pool.ctypes.data_as(C.POINTER(C.c_uint8)), pool.size, sc, len(scores), cs,
+        len(calls), sp, len(spans), out))
+    res, at = [], 0
+    for k in calls:
+        res.append([(int(out[at + q].whole), int(out[at + q].cut), int(out[at + q].cols))
+                    for q in range(len(k["texts"]))])
+        at += len(k["texts"])
+    return res

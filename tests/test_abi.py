@@ -46,6 +46,7 @@ def test_struct_layouts(lib):
     assert C.sizeof(_abi.BandedReadT) == 40
     assert C.sizeof(_abi.EndsT) == 40
     assert C.sizeof(_abi.HitT) == 40
+    assert C.sizeof(_abi.SortedCallT) == 80
     assert batch.JOB_DTYPE.itemsize == 80 and batch.RESULT_DTYPE.itemsize == 64
 
 

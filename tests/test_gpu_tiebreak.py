@@ -133,3 +133,47 @@ def test_banded_batch_long_reads():
         assert T.banded_batch(ctx, batch) == want
     finally:
         ctx.close()
+
+
+def test_sorted_batch_equals_sorted_calls():
+    """sf_sorted_batch (many segments' sorted calls in one batch) equals the oracle's
+    affine_sorted / affine_extend_sorted_cut_bonus call by call (align.rs:3245-3309
+    `sorted_batch_matches_single` inputs: sorted variants of a base sequence)."""
+    from spearfish_gb300 import build
+    build.build()
+    from spearfish_gb300 import batch as B, tiebreak as T
+    rng = np.random.default_rng(1803)
+    calls, want = [], []
+    for _ in range(60):
+        base = rng.integers(0, 4, int(rng.integers(1, 300))).tolist()
+        p = R.mutate(base, R.rand_edits(rng, int(rng.integers(0, 20)), max(1, len(base))))
+        variants = [(int(rng.integers(0, max(1, len(base)))),
+                     rng.integers(0, 4, int(rng.integers(0, 40))).tolist(),
+                     int(rng.integers(0, 60))) for _ in range(int(rng.integers(1, 8)))]
+        texts = R.sorted_texts(base, variants)
+        band = int(rng.integers(2, 40))
+        sci = int(rng.integers(0, 2))
+        sc = (R.ONT, R.HIFI)[sci]
+        if rng.random() < 0.4:
+            mode = int(rng.choice([R.GLOBAL, R.PREFIX]))
+            calls.append({"read": p, "texts": texts, "kind": T.SORTED_AFFINE, "mode": mode,
+                          "band": band, "sc_index": sci})
+            want.append([(x, x, 0) for x in (O.affine(p, t, mode, sc, band) for t in texts)])
+        else:
+            bonus, xd = int(rng.integers(0, 8)), int(rng.integers(5, 80))
+            diag = bool(rng.random() < 0.3)
+            w = max(len(t) for t in texts) + int(rng.integers(0, 40))
+            cut = None if rng.random() < 0.3 else int(rng.integers(0, w + 1))
+            track, within = bool(rng.random() < 0.8), bool(rng.random() < 0.5)
+            calls.append({"read": p, "texts": texts, "kind": T.SORTED_EXTEND_CUT, "band": band,
+                          "end_bonus": bonus, "xdrop": xd, "diagonal": diag, "window": w,
+                          "cut": cut, "track_cut": track, "bonus_within_cut": within,
+                          "sc_index": sci})
+            want.append([tuple(x) for x in O.affine_extend_sorted_cut_bonus(
+                p, texts, sc, band, bonus, xd, diag, w, cut, track, within)])
+    ctx = B.Context(0)
+    try:
+        got = T.sorted_batch(ctx, calls, scores=(R.ONT, R.HIFI))
+    finally:
+        ctx.close()
+    assert got == want
