@@ -114,7 +114,14 @@ int sf_affine_extend_window(const uint8_t *pattern, uint64_t m,
                             const sf_affine_t *sc, uint64_t band,
                             int32_t end_bonus, int32_t xdrop, sf_extend_t *out);
 
-/* align.rs:854-861 `affine_sorted`: results equal one `affine` per text. */
+/* align.rs:854-861 `affine_sorted`: results equal one `affine` per text.
+ * The sorted entry points (this, the two below and sf_sorted_batch) count
+ * DP work as align.rs:2210-2315 `affine_dp_sorted` does with its row sharing:
+ * a text's pass counts only the rows after those it shares with the previous
+ * text (same band shape, rows reading only the common prefix), and nothing
+ * when it takes the previous result.  On the GPU every pass runs separately
+ * by default; SF_SORTED_CHAINS=1 in the environment runs the passes that can
+ * share rows as chains that resume from row snapshots (same results). */
 int sf_affine_sorted(const uint8_t *pattern, uint64_t m,
                      const uint8_t *const *texts, const uint64_t *lens,
                      uint64_t count, int mode, const sf_affine_t *sc,

@@ -5,4 +5,7 @@ namespace sfk {
 cudaError_t launch_affine16_16(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {
   return launch_affine16_c<8>(tb, a, grid, block, s);
 }
+cudaError_t launch_affine16_chain_16(const AffLaunch& a, int grid, int block, cudaStream_t s) {
+  return launch_affine16_chain_c<8>(a, grid, block, s);
+}
 }  // namespace sfk

@@ -5,4 +5,7 @@ namespace sfk {
 cudaError_t launch_affine16_64(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {
   return launch_affine16_c<32>(tb, a, grid, block, s);
 }
+cudaError_t launch_affine16_chain_64(const AffLaunch& a, int grid, int block, cudaStream_t s) {
+  return launch_affine16_chain_c<32>(a, grid, block, s);
+}
 }  // namespace sfk

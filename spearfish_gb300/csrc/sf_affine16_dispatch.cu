@@ -71,4 +71,42 @@ cudaError_t launch_affine16h(int c, bool tb, const AffLaunch& a, int grid, int b
   }
 }
 
+cudaError_t launch_affine16_chain_4(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_6(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_8(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_10(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_12(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_14(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_16(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_20(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_24(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_28(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_32(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_40(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_48(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_56(const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16_chain_64(const AffLaunch&, int, int, cudaStream_t);
+
+cudaError_t launch_affine16_chain(int c, const AffLaunch& a, int grid, int block,
+                                  cudaStream_t s) {
+  switch (c) {
+    case 4: return launch_affine16_chain_4(a, grid, block, s);
+    case 6: return launch_affine16_chain_6(a, grid, block, s);
+    case 8: return launch_affine16_chain_8(a, grid, block, s);
+    case 10: return launch_affine16_chain_10(a, grid, block, s);
+    case 12: return launch_affine16_chain_12(a, grid, block, s);
+    case 14: return launch_affine16_chain_14(a, grid, block, s);
+    case 16: return launch_affine16_chain_16(a, grid, block, s);
+    case 20: return launch_affine16_chain_20(a, grid, block, s);
+    case 24: return launch_affine16_chain_24(a, grid, block, s);
+    case 28: return launch_affine16_chain_28(a, grid, block, s);
+    case 32: return launch_affine16_chain_32(a, grid, block, s);
+    case 40: return launch_affine16_chain_40(a, grid, block, s);
+    case 48: return launch_affine16_chain_48(a, grid, block, s);
+    case 56: return launch_affine16_chain_56(a, grid, block, s);
+    case 64: return launch_affine16_chain_64(a, grid, block, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace sfk

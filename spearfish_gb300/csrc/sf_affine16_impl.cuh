@@ -135,28 +135,21 @@ __device__ __forceinline__ void set_neg16(uint32_t (&h)[C2], uint32_t (&f)[C2], 
   static_assert(C2 <= 32, "set_neg16 covers 32 words per lane");
 }
 
-// DP_WORK cells of rows 1 .. R of a banded pass (align.rs:2573-2578): the sum of
-// hi_i - lo_i + 1 with lo_i = max(0, i - below), hi_i = min(i + above, n), rows whose band is
-// not empty.
-__device__ __forceinline__ uint64_t band_cells(int64_t R, int64_t below, int64_t above,
-                                               int64_t n) {
-  if (R <= 0) return 0;
-  const int64_t t = n - above;  // rows with i + above <= n
-  int64_t s1;                   // sum of hi_i
-  if (t >= R)
-    s1 = R * (R + 1) / 2 + R * above;
-  else if (t < 1)
-    s1 = R * n;
-  else
-    s1 = t * (t + 1) / 2 + t * above + (R - t) * n;
-  const int64_t u = R - below;  // rows with lo_i > 0
-  const int64_t s2 = u > 0 ? u * (u + 1) / 2 : 0;
-  return (uint64_t)(s1 - s2 + R);
-}
 
-template <int C2, bool TB>
-__device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
+// A chained pass (align.rs:2210-2315): the row it resumes after (0: from row 0) and that
+// row's slot; the chain's snapshot rows [base, want_end) of the want list, from `want` on the
+// ones this pass may save, and the chain's first slot (word offset in the arena).
+struct ChainRun {
+  int32_t resume = 0;
+  uint32_t base = 0, want = 0, want_end = 0;
+  uint64_t slot0 = 0;
+  uint32_t slot = 0;
+};
+
+template <int C2, bool TB, bool CH = false>
+__device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, int lane, const ChainRun cr) {
   constexpr int C = 2 * C2;
+  constexpr uint64_t kSlot = snap_slot_words(C2);
   constexpr int G = (C2 + 7) / 8;
   static_assert(2 * G == 2 * ((C + 15) / 16), "same traceback row size as the 32-bit kernel");
   // Rows of at most 8 words keep the sentinel's position as per-word masks; wider rows jump
@@ -222,6 +215,39 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   Book b;
   uint32_t pw = m > 0 ? __ldg(a.pool + x.J.p_word) >> 2 : 0;  // pattern bases from row 1
   uint2* tbp = TB ? reinterpret_cast<uint2*>(a.tb + x.J.tb_word) + lane : nullptr;
+  // Chained passes: rows first .. m, with row first - 1 restored from its snapshot
+  // (align.rs:2513-2524), and snapshots saved at the chain's rows from `wnext` on
+  // (align.rs:2631-2641).
+  int32_t first = 1;
+  uint32_t wnext = cr.want;
+  int32_t wrow = INT32_MAX;
+  if constexpr (CH) {
+    if (cr.resume > 0) {
+      const int32_t rr = cr.resume;
+      const uint32_t* s = a.snap + cr.slot0 + (uint64_t)cr.slot * kSlot;
+#pragma unroll
+      for (int k = 0; k < C2; ++k) {
+        h[k] = __ldcg(s + k * 32 + lane);
+        f[k] = __ldcg(s + (C2 + k) * 32 + lane);
+      }
+      off = (int32_t)__ldcg(s + 64 * C2);
+      b.clip_best = (int32_t)__ldcg(s + 64 * C2 + 1);
+      b.cut_best = (int32_t)__ldcg(s + 64 * C2 + 2);
+      b.ci = __ldcg(s + 64 * C2 + 3);
+      b.cj = __ldcg(s + 64 * C2 + 4);
+      g.range(rr, plo, phi);
+      // Row rr's text selectors (the band's columns from plo), and the pattern bases from
+      // row rr + 1.
+      Win<C> win;
+      win.load(a.pool, x.J.t_word, plo + kb);
+#pragma unroll
+      for (int k = 0; k < C2; ++k)
+        sel[k] = sel_byte(win.at(k)) | (sel_byte(win.at(C2 + k)) << 8);
+      pw = __ldg(a.pool + x.J.p_word + ((uint32_t)(rr + 1) >> 4)) >> (2u * ((uint32_t)(rr + 1) & 15u));
+      first = rr + 1;
+    }
+    wrow = wnext < cr.want_end ? (int32_t)__ldg(a.want + wnext) : INT32_MAX;
+  }
 
   // One row.  D1: lo moved right by one (offset K reads the previous row at K + 1 above and
   // K diagonally); else lo stayed (K above, K - 1 diagonally; lo = 0, column 0 in lane 0).
@@ -384,6 +410,25 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
     }
     plo = lo;
     phi = hi;
+    if constexpr (CH) {
+      if (i == wrow) {
+        uint32_t* s = a.snap + cr.slot0 + (uint64_t)(wnext - cr.base) * kSlot;
+#pragma unroll
+        for (int k = 0; k < C2; ++k) {
+          __stcg(s + k * 32 + lane, h[k]);
+          __stcg(s + (C2 + k) * 32 + lane, f[k]);
+        }
+        if (lane == 0) {
+          __stcg(s + 64 * C2, (uint32_t)off);
+          __stcg(s + 64 * C2 + 1, (uint32_t)b.clip_best);
+          __stcg(s + 64 * C2 + 2, (uint32_t)b.cut_best);
+          __stcg(s + 64 * C2 + 3, b.ci);
+          __stcg(s + 64 * C2 + 4, b.cj);
+        }
+        ++wnext;
+        wrow = wnext < cr.want_end ? (int32_t)__ldg(a.want + wnext) : INT32_MAX;
+      }
+    }
     return false;
   };
 
@@ -392,8 +437,9 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
   const int32_t endA = m < g.below ? m : g.below;
   const int64_t lastB = (int64_t)n + g.below;  // the last row whose band is not empty
   const int32_t endB = (int64_t)m < lastB ? m : (int32_t)lastB;
-  for (int32_t i = 1; i <= endA && !stopped; ++i) stopped = row(i, std::false_type{});
-  for (int32_t i = endA + 1; i <= endB && !stopped; ++i) stopped = row(i, std::true_type{});
+  for (int32_t i = first; i <= endA && !stopped; ++i) stopped = row(i, std::false_type{});
+  for (int32_t i = max(endA + 1, first); i <= endB && !stopped; ++i)
+    stopped = row(i, std::true_type{});
   if (!stopped && endB < m) {
     // Row endB + 1 lies past the text: the pass ends there with no score (align.rs:2543-2553).
     r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)(endB + 1),
@@ -432,6 +478,7 @@ __device__ void pair16(const sfk::AffLaunch& a, uint32_t jid, int lane) {
     walk_lean(a, jid, tb_layout<C>(false, true, x.J, x.P.flags), x.J, x.P.flags, r, lane);
   }
   __syncwarp();
+  return r;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -792,7 +839,7 @@ __global__ void __launch_bounds__(128, (C2 == 8 || C2 >= 10) ? 3 : 4)
 
 template <int C2>
 struct MinBlocks16 {
-  static constexpr int value = C2 <= 8 ? 6 : (C2 <= 10 ? 4 : (C2 <= 16 ? 3 : 2));
+  static constexpr int value = min_blocks16(C2);
 };
 
 template <int C2, bool TB>
@@ -803,7 +850,53 @@ __global__ void __launch_bounds__(128, MinBlocks16<C2>::value) affine16_kernel(s
     if (lane == 0) q = atomicAdd(a.counter, 1u);
     q = __shfl_sync(FULL, q, 0);
     if (q >= a.njobs) break;
-    pair16<C2, TB>(a, a.order[q], lane);
+    pair16<C2, TB>(a, a.order[q], lane, ChainRun{});
+  }
+}
+
+// One chain of sorted texts (align.rs:2210-2315 `affine_dp_sorted`), its passes in order.
+// A pass whose text agrees with the previous one over every base that pass read, with a
+// band of the same shape, takes its result (align.rs:2262-2266); so does one that would
+// resume within rows the previous pass never got past (2283-2285); the others resume from
+// the snapshot of their shared rows.  Every pass reports the rows and cells of its whole
+// pass; the host counts the rows the reference computes.
+template <int C2>
+__device__ __forceinline__ void chain16(const sfk::AffLaunch& a, const DChain& ch, int lane) {
+  DRes prev{};
+  uint32_t n_prev = 0;
+  for (uint32_t u = 0; u < ch.count; ++u) {
+    const uint32_t jid = ch.first + u;
+    const DLink L = a.links[jid];
+    const uint32_t n = a.jobs[jid].n;
+    const bool clip = (a.params[jid].flags & F_CLIP) != 0;
+    const uint32_t tr = prev.text_read;
+    const bool same = u > 0 && clip && L.same_shape && tr < n_prev && tr < n && tr <= L.lcp;
+    if (same || (u > 0 && L.resume > 0 && prev.last_row <= L.resume)) {
+      if (lane == 0) a.out[jid] = prev;
+    } else {
+      ChainRun cr;
+      cr.resume = u > 0 ? (int32_t)L.resume : 0;
+      cr.slot = L.slot;
+      cr.base = ch.want;
+      cr.want = ch.want + (cr.resume > 0 ? L.slot + 1 : 0);
+      cr.want_end = ch.want + ch.n_want;
+      cr.slot0 = ch.snap_word;
+      prev = pair16<C2, false, true>(a, jid, lane, cr);
+    }
+    n_prev = n;
+  }
+}
+
+template <int C2>
+__global__ void __launch_bounds__(128, MinBlocks16<C2>::value)
+    affine16_chain_kernel(sfk::AffLaunch a) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t q = 0;
+    if (lane == 0) q = atomicAdd(a.counter, 1u);
+    q = __shfl_sync(FULL, q, 0);
+    if (q >= a.njobs) break;
+    chain16<C2>(a, a.chains[a.order[q]], lane);
   }
 }
 
@@ -817,6 +910,12 @@ cudaError_t launch_affine16h_c(bool tb, const AffLaunch& a, int grid, int block,
     affine16h_kernel<C2, true><<<grid, block, 0, s>>>(a);
   else
     affine16h_kernel<C2, false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int C2>
+cudaError_t launch_affine16_chain_c(const AffLaunch& a, int grid, int block, cudaStream_t s) {
+  affine16_chain_kernel<C2><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -97,8 +97,15 @@ struct PinBuf {
 
 // ---- passes ----------------------------------------------------------------------------
 
-// PK_AFFINE16 only classifies buckets: an affine pass the packed 16-bit kernel runs.
-enum PassKind : uint8_t { PK_MYERS = 0, PK_AFFINE = 1, PK_LOCAL = 2, PK_AFFINE16 = 3 };
+// PK_AFFINE16 and PK_CHAIN16 only classify buckets: an affine pass the packed 16-bit kernel
+// runs, and a chain of sorted-text passes it runs in order.
+enum PassKind : uint8_t {
+  PK_MYERS = 0,
+  PK_AFFINE = 1,
+  PK_LOCAL = 2,
+  PK_AFFINE16 = 3,
+  PK_CHAIN16 = 4
+};
 
 // One DP pass as the reference's `affine_dp` / `distance` / `local_band_core` receive it.
 struct Pass {
@@ -113,6 +120,12 @@ struct Pass {
   int64_t dlo = 0, dhi = 0;
   uint32_t k = SF_NONE;
   sf_affine_t sc{2, 4, 4, 2};
+  // Sorted texts (align.rs:2210-2315 `affine_dp_sorted`): on a chain's first pass, how many
+  // consecutive passes the chain holds; on each chained pass, the row its pass resumes after
+  // (0: none), the common prefix of its text with the previous one and whether both bands
+  // have the same shape.
+  uint32_t chain = 0, resume = 0, lcp = 0;
+  bool same_shape = false;
 };
 
 // A kernel class: what a pass runs on (kind, cells or blocks per lane, wide rows,
@@ -141,6 +154,8 @@ struct Bucket {
   uint32_t first = 0, count = 0;  // range in the order array
   int grid = 0, block = 128;
   uint64_t scratch_off = 0;       // wide rows: this bucket's slice of the scratch (int32s)
+  uint64_t work = 0;              // estimated work (cells of its passes' widest rows)
+  int stream = 0;                 // auxiliary stream it runs on
 };
 
 }  // namespace sfe
@@ -168,7 +183,12 @@ struct sf_plan {
   std::string desc;
   // Device buffers.
   DevBuf d_bytes, d_pool, d_seq, d_djobs, d_params, d_res, d_mjobs, d_mout, d_tjobs, d_tres,
-      d_tb, d_ops, d_opsc, d_offs, d_order, d_counters, d_wlist, d_cls, d_scratch, d_total;
+      d_tb, d_ops, d_opsc, d_offs, d_order, d_counters, d_wlist, d_cls, d_scratch, d_total,
+      d_chains, d_links, d_want, d_snap;
+  // Chains of sorted-call passes the plan runs on the chain kernel, their passes, and per
+  // pass whether it is one of them.
+  uint32_t n_chains = 0, n_chained = 0;
+  std::vector<uint8_t> chained;
   // Pinned staging.
   PinBuf h_stage, h_res, h_mout, h_tres, h_ops, h_total;
   cudaGraphExec_t graph = nullptr;

@@ -100,6 +100,15 @@ int default_lanes16() {
   return env && env[0] == '1' && env[1] == '6' ? 16 : 32;
 }
 
+// Row sharing between sorted texts on the GPU: SF_SORTED_CHAINS=1 in the environment runs
+// the passes of a sorted call that can share rows as chains; by default every pass runs
+// separately (the results are the same either way, and separate passes finish sooner on the
+// batches measured: a chain runs its passes one after another); read once per plan.
+bool allow_chains() {
+  const char* env = std::getenv("SF_SORTED_CHAINS");
+  return env && env[0] == '1';
+}
+
 // Kernel class of an affine or local pass: the packed 16-bit kernel when the pass fits it,
 // else the 32-bit register kernel, else (rows wider than 32 * 48 cells) the wide-row kernel.
 void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, PassKind& kind,
@@ -263,6 +272,60 @@ int plan_build(sf_plan* P) {
   const int lanes16 = default_lanes16();
   const TuneTable* tune = P->tune_override ? P->tune_override : &ctx->tune;
   P->store = ctx->store;
+  // Sorted calls the chain kernel takes (Pass::chain on a call's first pass), when chains
+  // are on: every pass a 16-bit Global / Prefix pass without traceback, on the class of the
+  // call's widest row.  A call's passes form chains, each starting at a pass that resumes
+  // nothing (it depends on no earlier pass), which one warp runs in order.  Chains of one
+  // pass, and chains whose snapshots would pass the arena's cap, run as separate passes.
+  struct Sub {
+    size_t first;
+    uint32_t count;
+    int c;
+  };
+  std::vector<Sub> subs;
+  P->chained.assign(np, 0);
+  {
+    constexpr uint64_t kSnapCapWords = (uint64_t(1) << 30) / 4;
+    uint64_t snap_total = 0;
+    const bool on = use16 && allow_chains();
+    for (size_t q = 0; on && q < np;) {
+      const uint32_t cnt = P->passes[q].chain;
+      if (cnt < 2 || cnt > np - q) {
+        ++q;
+        continue;
+      }
+      int64_t wm = 0;
+      bool ok = true;
+      for (size_t u = q; u < q + cnt && ok; ++u) {
+        const Pass& p = P->passes[u];
+        uint32_t fl = 0;
+        const DJob j = make_djob(p, fl);
+        const int64_t w = band_wmax(j, fl);
+        ok = p.kind == PK_AFFINE && !p.want_cigar && fits16(p, fl, w) &&
+             (!p.resume || (u > q && p.resume < p.m));
+        wm = std::max(wm, w);
+      }
+      int c = 0;
+      for (int k = 0; ok && k < sfk::kAffine16NC; ++k)
+        if (32 * (int64_t)sfk::kAffine16C[k] >= wm) {
+          c = sfk::kAffine16C[k];
+          break;
+        }
+      for (size_t h = q; c && h < q + cnt;) {
+        size_t e = h + 1;
+        while (e < q + cnt && P->passes[e].resume) ++e;
+        const uint64_t words = (e - h - 1) * snap_slot_words(c / 2);  // at most one per pass
+        if (e - h >= 2 && snap_total + words <= kSnapCapWords) {
+          snap_total += words;
+          subs.push_back(Sub{h, (uint32_t)(e - h), c});
+          for (size_t u = h; u < e; ++u) P->chained[u] = 1;
+        }
+        h = e;
+      }
+      q += cnt;
+    }
+  }
+  std::vector<uint64_t> pass_work(np, 0);
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
@@ -324,12 +387,53 @@ int plan_build(sf_plan* P) {
     }
     P->slot[q] = (uint32_t)dj.size();
     const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
-    items.push_back({Key2{kind, c, wide, tb, ln}, Item{(uint32_t)dj.size(), work}});
+    pass_work[q] = work;
+    if (!P->chained[q]) items.push_back({Key2{kind, c, wide, tb, ln}, Item{(uint32_t)dj.size(), work}});
     dj.push_back(j);
     dp.push_back(pr);
     tj.push_back(t);
     cls.push_back((uint16_t)(c | (wide ? 0x100 : 0) | (kind == PK_AFFINE16 ? 0x200 : 0)));
   }
+  // Chains: one work item each (longest first, as passes); per chained job its link; per
+  // chain its snapshot rows, the sorted distinct resume rows (align.rs:2244-2246), and a
+  // slot for each.
+  std::vector<DChain> chains;
+  std::vector<DLink> links;
+  std::vector<uint32_t> want;
+  uint64_t snap_words = 0;
+  uint32_t n_chained = 0;
+  for (const Sub& sb : subs) {
+    if (links.empty()) links.assign(dj.size(), DLink{});
+    DChain ch{};
+    ch.first = P->slot[sb.first];
+    ch.count = sb.count;
+    ch.want = (uint32_t)want.size();
+    ch.snap_word = snap_words;
+    std::vector<uint32_t> rows;
+    uint64_t work = 0;
+    for (size_t u = sb.first; u < sb.first + sb.count; ++u) {
+      if (u > sb.first) rows.push_back(P->passes[u].resume);
+      work += pass_work[u];
+    }
+    std::sort(rows.begin(), rows.end());
+    rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+    ch.n_want = (uint32_t)rows.size();
+    for (size_t u = sb.first; u < sb.first + sb.count; ++u) {
+      const Pass& p = P->passes[u];
+      DLink& L = links[P->slot[u]];
+      L.resume = u > sb.first ? p.resume : 0;
+      L.slot = L.resume ? (uint32_t)(std::lower_bound(rows.begin(), rows.end(), L.resume) - rows.begin()) : 0;
+      L.lcp = p.lcp;
+      L.same_shape = p.same_shape ? 1u : 0u;
+    }
+    want.insert(want.end(), rows.begin(), rows.end());
+    snap_words += rows.size() * snap_slot_words(sb.c / 2);
+    items.push_back({Key2{PK_CHAIN16, sb.c, 0, 0, 32}, Item{(uint32_t)chains.size(), work}});
+    chains.push_back(ch);
+    n_chained += sb.count;
+  }
+  P->n_chains = (uint32_t)chains.size();
+  P->n_chained = n_chained;
   P->n_aff = (uint32_t)dj.size();
   P->n_my = (uint32_t)mj.size();
   P->n_walk = (uint32_t)wlist.size();
@@ -395,6 +499,7 @@ int plan_build(sf_plan* P) {
     b.lanes = sorted_keys[u].lanes;
     b.first = (uint32_t)start[u];
     b.count = (uint32_t)(start[u + 1] - start[u]);
+    b.work = bwork[u];
     P->buckets.push_back(b);
     for (auto it = b0; it != b1; ++it) order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
   }
@@ -411,7 +516,7 @@ int plan_build(sf_plan* P) {
       b.grid = (int)std::min<uint64_t>((warps + wpb - 1) / wpb, (uint64_t)ctx->sms * (2048 / b.block));
     } else {
       b.block = 128;
-      const uint64_t per_block = b.lanes == 16 ? 8 : 4;  // passes a 4-warp block holds
+      const uint64_t per_block = b.lanes == 16 ? 8 : 4;  // passes (chains) a 4-warp block holds
       const uint64_t blocks = (b.count + per_block - 1) / per_block;
       const uint64_t cap = b.wide ? (uint64_t)ctx->sms * 2 : (uint64_t)ctx->sms * 16;
       b.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, cap));
@@ -423,6 +528,8 @@ int plan_build(sf_plan* P) {
     }
   }
   P->wide_warps = wide_warps;
+  // Streams: round robin over the buckets in key order, so that their tails overlap.
+  for (size_t u = 0; u < P->buckets.size(); ++u) P->buckets[u].stream = (int)(u % sf_context::kAux);
   // Device buffers.
   int rc;
   if ((rc = P->d_bytes.ensure(std::max<uint64_t>(P->pool_bytes, 16)))) return rc;
@@ -446,10 +553,16 @@ int plan_build(sf_plan* P) {
   if ((rc = P->d_counters.ensure(P->buckets.size() * 4 + 64))) return rc;
   if ((rc = P->d_wlist.ensure(wlist.size() * 4 + 64))) return rc;
   if ((rc = P->d_scratch.ensure(scratch_total * 4 + 64))) return rc;
+  if ((rc = P->d_chains.ensure(chains.size() * sizeof(DChain) + 64))) return rc;
+  if ((rc = P->d_links.ensure(links.size() * sizeof(DLink) + 64))) return rc;
+  if ((rc = P->d_want.ensure(want.size() * 4 + 64))) return rc;
+  if ((rc = P->d_snap.ensure(snap_words * 4 + 64))) return rc;
   // Descriptors -> device (one pinned staging area, one stream).
   const size_t seq_bytes = nseq * 20;
   const size_t total = seq_bytes + dj.size() * (sizeof(DJob) + sizeof(DParams) + sizeof(TJob) + 1) +
-                       mj.size() * sizeof(MJob) + order.size() * 4 + wlist.size() * 4 + 1024;
+                       mj.size() * sizeof(MJob) + order.size() * 4 + wlist.size() * 4 +
+                       chains.size() * sizeof(DChain) + links.size() * sizeof(DLink) +
+                       want.size() * 4 + 1024;
   if ((rc = P->h_stage.ensure(total))) return rc;
   uint8_t* h = P->h_stage.as<uint8_t>();
   size_t at = 0;
@@ -475,6 +588,9 @@ int plan_build(sf_plan* P) {
   if ((rc = put(P->d_mjobs, mj.data(), mj.size() * sizeof(MJob)))) return rc;
   if ((rc = put(P->d_order, order.data(), order.size() * 4))) return rc;
   if ((rc = put(P->d_wlist, wlist.data(), wlist.size() * 4))) return rc;
+  if ((rc = put(P->d_chains, chains.data(), chains.size() * sizeof(DChain)))) return rc;
+  if ((rc = put(P->d_links, links.data(), links.size() * sizeof(DLink)))) return rc;
+  if ((rc = put(P->d_want, want.data(), want.size() * 4))) return rc;
   // The pool's slack words stay zero.
   CK(cudaMemsetAsync(P->d_pool.p, 0, P->pool_words * 4, ctx->s));
   CK(cudaStreamSynchronize(ctx->s));  // staging is reused by the next upload
@@ -492,15 +608,20 @@ int plan_build(sf_plan* P) {
                   "%s{\"kind\": \"%s\", \"c\": %d, \"wide\": %s, \"traceback\": %s, \"lanes\": %d, "
                   "\"jobs\": %u, \"grid\": %d, \"block\": %d, \"work\": %llu}",
                   q ? ", " : "",
-                  b.kind == PK_MYERS ? "myers"
-                                     : (b.kind == PK_LOCAL ? "local"
-                                                           : (b.kind == PK_AFFINE16 ? "affine16" : "affine")),
+                  b.kind == PK_MYERS     ? "myers"
+                  : b.kind == PK_LOCAL   ? "local"
+                  : b.kind == PK_AFFINE16 ? "affine16"
+                  : b.kind == PK_CHAIN16 ? "chain16"
+                                         : "affine",
                   b.c,
                   b.wide ? "true" : "false", b.tb ? "true" : "false", b.lanes, b.count, b.grid,
                   b.block, (unsigned long long)bwork[q]);
     d += buf;
   }
-  d += "], \"pool_words\": " + std::to_string(P->pool_words) +
+  d += "], \"chains\": " + std::to_string(P->n_chains) +
+       ", \"chained_passes\": " + std::to_string(n_chained) +
+       ", \"snapshot_bytes\": " + std::to_string(snap_words * 4) +
+       ", \"pool_words\": " + std::to_string(P->pool_words) +
        ", \"traceback_bytes\": " + std::to_string(tb_words * 4) + "}";
   P->desc = d;
   return SF_OK;
@@ -538,14 +659,16 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
   if ((mrc = mark())) return mrc;
   // Buckets fan out over the auxiliary streams so that their tails overlap.
   const int nb = (int)P->buckets.size();
-  const int fan = evs ? 1 : std::min(nb, sf_context::kAux);
-  if (fan > 1) CK(cudaEventRecord(ctx->fork, s));
+  const bool fan = !evs && nb > 1;
+  bool used[sf_context::kAux] = {};
+  if (fan) CK(cudaEventRecord(ctx->fork, s));
   for (int q = 0; q < nb; ++q) {
     const Bucket& b = P->buckets[q];
     cudaStream_t bs = s;
-    if (fan > 1) {
-      bs = ctx->aux[q % fan];
-      if (q < fan) CK(cudaStreamWaitEvent(bs, ctx->fork, 0));
+    if (fan) {
+      bs = ctx->aux[b.stream];
+      if (!used[b.stream]) CK(cudaStreamWaitEvent(bs, ctx->fork, 0));
+      used[b.stream] = true;
     }
     uint32_t* counter = P->d_counters.as<uint32_t>() + q;
     const uint32_t* order = P->d_order.as<uint32_t>() + b.first;
@@ -575,7 +698,13 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
       al.tjobs = P->d_tjobs.as<TJob>();
       al.ops = P->d_ops.as<uint32_t>();
       al.tres = P->d_tres.as<TRes>();
-      if (b.kind == PK_AFFINE16 && b.lanes == 16)
+      al.chains = P->d_chains.as<DChain>();
+      al.links = P->d_links.as<DLink>();
+      al.want = P->d_want.as<uint32_t>();
+      al.snap = P->d_snap.as<uint32_t>();
+      if (b.kind == PK_CHAIN16)
+        CK(sfk::launch_affine16_chain(b.c, al, b.grid, b.block, bs));
+      else if (b.kind == PK_AFFINE16 && b.lanes == 16)
         CK(sfk::launch_affine16h(b.c, b.tb, al, b.grid, b.block, bs));
       else if (b.kind == PK_AFFINE16)
         CK(sfk::launch_affine16(b.c, b.tb, al, b.grid, b.block, bs));
@@ -585,8 +714,9 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
     launches++;
     if ((mrc = mark())) return mrc;
   }
-  if (fan > 1) {
-    for (int i = 0; i < fan; ++i) {
+  if (fan) {
+    for (int i = 0; i < sf_context::kAux; ++i) {
+      if (!used[i]) continue;
       CK(cudaEventRecord(ctx->join[i], ctx->aux[i]));
       CK(cudaStreamWaitEvent(s, ctx->join[i], 0));
     }
@@ -810,6 +940,64 @@ Pass affine_pass(uint64_t p_off, uint64_t m, uint64_t t_off, uint64_t n, int mod
   p.geom = n;
   p.sc = *sc;
   return p;
+}
+
+// align.rs:2229-2243: passes [q0, q0 + count) of `ps` hold one pattern against sorted texts
+// with one mode, band, clip and geometry rule.  Marks them as one sorted call and sets, per
+// pass, the rows it shares with the previous text's pass (rows i read text bases below
+// i + above, so rows with i + above <= the common prefix agree; the last row is always
+// computed), the common prefix and whether both bands have the same shape.  text(u) gives
+// pass u's text bytes.  Unbanded passes share nothing.
+template <class F>
+void link_sorted(std::vector<Pass>& ps, size_t q0, size_t count, F text) {
+  if (count < 2) return;
+  if (ps[q0].mode == SF_INFIX || ps[q0].band == SF_NOLIMIT) return;
+  auto shape = [](const Pass& p) {
+    return std::make_pair(usat_add(p.band, usat_sub(p.m, p.geom)),
+                          usat_add(p.band, usat_sub(p.geom, p.m)));
+  };
+  ps[q0].chain = (uint32_t)count;
+  for (size_t k = 1; k < count; ++k) {
+    Pass& p = ps[q0 + k];
+    const Pass& pp = ps[q0 + k - 1];
+    const uint8_t* a = text(q0 + k);
+    const uint8_t* b = text(q0 + k - 1);
+    const uint64_t lim = std::min<uint64_t>(p.n, pp.n);
+    uint64_t l = 0;
+    while (l < lim && a[l] == b[l]) ++l;
+    p.lcp = (uint32_t)l;
+    p.same_shape = shape(p) == shape(pp);
+    p.resume = p.same_shape
+                   ? (uint32_t)std::min<uint64_t>(usat_sub(l, shape(p).second), usat_sub(p.m, 1))
+                   : 0;
+  }
+}
+
+// align.rs:2248-2310 with 2571-2576: the DP work the reference counts for one sorted call,
+// from its passes' whole-pass results res(u) (every result equals the separate pass's).  A
+// pass takes the previous text's result when that pass read nothing the two texts differ in
+// (with clip) or stopped within the rows they share, and counts nothing; else it counts the
+// rows after its resume row.
+template <class R>
+void count_sorted(const std::vector<Pass>& ps, size_t q0, size_t count, R res) {
+  const bool full = count && (ps[q0].mode == SF_INFIX || ps[q0].band == SF_NOLIMIT);
+  size_t src = q0;  // the pass whose result the previous text took
+  for (size_t k = 0; k < count; ++k) {
+    const Pass& p = ps[q0 + k];
+    if (k > 0) {
+      const DRes& o = res(src);
+      const uint32_t tr = o.text_read;
+      const bool same = p.clip && !full && p.same_shape && tr < ps[q0 + k - 1].n && tr < p.n &&
+                        tr <= p.lcp;
+      if (same || (p.resume > 0 && o.last_row <= p.resume)) continue;
+    }
+    src = q0 + k;
+    const DRes& d = res(src);
+    uint32_t flags = 0;
+    const DJob j = make_djob(p, flags);
+    g_dp_rows += d.rows - p.resume;
+    g_dp_cells += d.cells - band_cells(p.resume, j.below, j.above, p.n);
+  }
 }
 
 int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
@@ -1153,10 +1341,11 @@ int sf_affine_sorted(const uint8_t* pattern, uint64_t m, const uint8_t* const* t
     const uint64_t to = g.add(texts[q], lens[q]);
     ps.push_back(affine_pass(po, m, to, lens[q], mode, sc, band));
   }
+  link_sorted(ps, 0, count, [&](size_t u) { return texts[u]; });
   std::vector<DRes> r;
   int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
   if (rc) return rc;
-  count_dp(ps, r);
+  count_sorted(ps, 0, count, [&](size_t u) -> const DRes& { return r[u]; });
   for (uint64_t q = 0; q < count; ++q) out[q] = r[q].score;
   return SF_OK;
 }
@@ -1185,10 +1374,11 @@ int sf_affine_extend_sorted_cut_bonus(const uint8_t* pattern, uint64_t m,
     p.cut = cut;
     ps.push_back(p);
   }
+  link_sorted(ps, 0, count, [&](size_t u) { return texts[u]; });
   std::vector<DRes> r;
   int rc = run_passes(ps, g, &r, nullptr, nullptr, nullptr, nullptr);
   if (rc) return rc;
-  count_dp(ps, r);
+  count_sorted(ps, 0, count, [&](size_t u) -> const DRes& { return r[u]; });
   for (uint64_t q = 0; q < count; ++q) {
     // align.rs:929-948
     const DRes& d = r[q];
@@ -1649,6 +1839,7 @@ int sf_sorted_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
       return fail(SF_ERR_INVALID, "pattern outside the pool");
     if (k.m >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
     const sf_affine_t* sc = &scores[k.sc_index];
+    const size_t q0 = ps.size();
     for (uint64_t q = 0; q < k.count; ++q) {
       const sf_span_t& t = texts[k.first + q];
       if (t.off > pool_bytes || t.len > pool_bytes - t.off)
@@ -1669,6 +1860,7 @@ int sf_sorted_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
       }
       text_of.push_back(k.first + q);
     }
+    link_sorted(ps, q0, k.count, [&](size_t u) { return pool + texts[text_of[u]].off; });
   }
   if (ps.empty()) return SF_OK;
   if (!ctx->cache) {
@@ -1687,6 +1879,7 @@ int sf_sorted_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
   size_t u = 0;
   for (uint64_t c = 0; c < n_calls; ++c) {
     const sf_sorted_call_t& k = calls[c];
+    count_sorted(P->passes, u, k.count, [&](size_t v) -> const DRes& { return rs[P->slot[v]]; });
     for (uint64_t q = 0; q < k.count; ++q, ++u) {
       const DRes& d = rs[P->slot[u]];
       sf_cut_t& o = out[text_of[u]];

@@ -76,6 +76,33 @@ struct TRes {
   uint32_t end_i, end_j, text_start, n_ops;
 };
 
+// Sorted texts against one pattern (align.rs:2210-2315 `affine_dp_sorted`): a chain of
+// consecutive jobs that one warp runs in order, each resuming from a row snapshot of an
+// earlier one where the texts share the bases those rows read.  A chain starts at a pass
+// that resumes nothing.
+struct DChain {
+  uint32_t first, count;   // jobs [first, first + count)
+  uint32_t want, n_want;   // snapshot rows: want list [want, want + n_want), ascending
+  uint64_t snap_word;      // the chain's n_want snapshot slots in the snapshot arena
+};
+
+// Per chained job: the row it resumes after (0: none) and that row's slot, the common
+// prefix with the previous text and whether both bands have the same shape
+// (align.rs:2229-2243).
+struct DLink {
+  uint32_t resume, slot, lcp, same_shape;
+};
+
+// 4-warp blocks of the 16-bit register kernel resident per SM (its launch bounds), by words
+// per lane.
+__host__ __device__ constexpr int min_blocks16(int c2) {
+  return c2 <= 8 ? 6 : (c2 <= 10 ? 4 : (c2 <= 16 ? 3 : 2));
+}
+
+// A snapshot slot of the 16-bit kernel with C2 words per lane: H words, F words (word k of
+// lane l at k * 32 + l), then the offset and the clip state (align.rs:2130-2148 `Snap`).
+__host__ __device__ constexpr uint64_t snap_slot_words(int c2) { return (uint64_t)64 * c2 + 32; }
+
 // Traceback words per lane and row: two bit-plane words per group of 16 cells, stored as one
 // 8-byte pair (A, B) per lane and group, lane-fastest: pair g*32 + lane of the row.
 __host__ __device__ inline uint32_t tb_words_per_lane(int c) { return (uint32_t)(2 * ((c + 15) / 16)); }
@@ -103,6 +130,25 @@ __host__ __device__ inline uint64_t tb_row_words(int c, int64_t chunks) {
 // Chunks of 32*C offsets a wide row needs: its cells plus the NEG sentinel after them.
 __host__ __device__ inline int64_t wide_chunks(int c, int64_t w) {
   return (w + 1 + 32 * c - 1) / (32 * c);
+}
+
+// DP_WORK cells of rows 1 .. R of a banded pass (align.rs:2573-2578): the sum of
+// hi_i - lo_i + 1 with lo_i = max(0, i - below), hi_i = min(i + above, n), rows whose band is
+// not empty.
+__host__ __device__ inline uint64_t band_cells(int64_t R, int64_t below, int64_t above,
+                                               int64_t n) {
+  if (R <= 0) return 0;
+  const int64_t t = n - above;  // rows with i + above <= n
+  int64_t s1;                   // sum of hi_i
+  if (t >= R)
+    s1 = R * (R + 1) / 2 + R * above;
+  else if (t < 1)
+    s1 = R * n;
+  else
+    s1 = t * (t + 1) / 2 + t * above + (R - t) * n;
+  const int64_t u = R - below;  // rows with lo_i > 0
+  const int64_t s2 = u > 0 ? u * (u + 1) / 2 : 0;
+  return (uint64_t)(s1 - s2 + R);
 }
 
 __device__ __forceinline__ uint32_t base_at(const uint32_t* __restrict__ pool, uint64_t word,
@@ -146,6 +192,11 @@ struct AffLaunch {
   const sf::TJob* tjobs;      // traceback: end cell kind and CIGAR slot per job
   uint32_t* ops;              // CIGAR slots
   sf::TRes* tres;             // walk results
+  // Chain buckets (sorted texts): `order` holds chain indices.
+  const sf::DChain* chains;
+  const sf::DLink* links;     // per job
+  const uint32_t* want;       // snapshot rows of every chain
+  uint32_t* snap;             // snapshot arena
 };
 
 // C: cells per lane (register rows); wide: rows in global scratch, chunked.
@@ -165,6 +216,9 @@ cudaError_t launch_affine16h(int c, bool tb, const AffLaunch& a, int grid, int b
                              cudaStream_t s);
 extern const int kAffine16HC[];
 extern const int kAffine16HNC;
+// Chains of sorted texts on the 16-bit register kernel (C from kAffine16C, no traceback).
+cudaError_t launch_affine16_chain(int c, const AffLaunch& a, int grid, int block,
+                                  cudaStream_t s);
 
 
 struct MyersLaunch {
