@@ -136,6 +136,32 @@ __device__ __forceinline__ void set_neg16(uint32_t (&h)[C2], uint32_t (&f)[C2], 
 }
 
 
+// Sets word k's fields selected by ms (H and F) to NEG; k is the same in every lane (a
+// uniform jump), ms is zero in the lanes that hold no field to set.
+template <int C2>
+__device__ __forceinline__ void set_word16(uint32_t (&h)[C2], uint32_t (&f)[C2], int k,
+                                           uint32_t ms) {
+  switch (k) {
+#define SF_WORD16_CASE(q)                     \
+  case q:                                     \
+    if constexpr (q < C2) {                   \
+      h[q] = (h[q] & ~ms) | (kNeg2 & ms);     \
+      f[q] = (f[q] & ~ms) | (kNeg2 & ms);     \
+    }                                         \
+    break;
+    SF_WORD16_CASE(0) SF_WORD16_CASE(1) SF_WORD16_CASE(2) SF_WORD16_CASE(3) SF_WORD16_CASE(4)
+    SF_WORD16_CASE(5) SF_WORD16_CASE(6) SF_WORD16_CASE(7) SF_WORD16_CASE(8) SF_WORD16_CASE(9)
+    SF_WORD16_CASE(10) SF_WORD16_CASE(11) SF_WORD16_CASE(12) SF_WORD16_CASE(13) SF_WORD16_CASE(14)
+    SF_WORD16_CASE(15) SF_WORD16_CASE(16) SF_WORD16_CASE(17) SF_WORD16_CASE(18) SF_WORD16_CASE(19)
+    SF_WORD16_CASE(20) SF_WORD16_CASE(21) SF_WORD16_CASE(22) SF_WORD16_CASE(23) SF_WORD16_CASE(24)
+    SF_WORD16_CASE(25) SF_WORD16_CASE(26) SF_WORD16_CASE(27) SF_WORD16_CASE(28) SF_WORD16_CASE(29)
+    SF_WORD16_CASE(30) SF_WORD16_CASE(31)
+#undef SF_WORD16_CASE
+    default:
+      break;
+  }
+}
+
 // A chained pass (align.rs:2210-2315): the row it resumes after (0: from row 0) and that
 // row's slot; the chain's snapshot rows [base, want_end) of the want list, from `want` on the
 // ones this pass may save, and the chain's first slot (word offset in the arena).
@@ -252,11 +278,18 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
   // One row.  D1: lo moved right by one (offset K reads the previous row at K + 1 above and
   // K diagonally); else lo stayed (K above, K - 1 diagonally; lo = 0, column 0 in lane 0).
   // Returns true when the pass stops at this row.
-  auto row = [&](int32_t i, auto d1tag) -> bool {
-    constexpr bool D1 = decltype(d1tag)::value;
+  // Rows whose band lies inside the text (lo > 0, i + above <= n) all have the width
+  // below + above + 1: their sentinel sits in one word of one lane (ks, ms).
+  int32_t Wc = 0, ks = 0;
+  uint32_t ms = 0;
+  bool sent = false;
+  auto row = [&](int32_t i, auto modetag) -> bool {
+    // MODE 0: lo = 0; 1: lo moves right by one; 2: as 1, with i + above <= n.
+    constexpr int MODE = decltype(modetag)::value;
+    constexpr bool D1 = MODE >= 1, ST = MODE == 2;
     // align.rs:2462-2468; rows past n + below (empty) never get here.
-    const int32_t lo = D1 ? i - g.below : 0, hi = min(i + g.above, n);
-    const int32_t W = hi - lo + 1;
+    const int32_t lo = D1 ? i - g.below : 0, hi = ST ? i + g.above : min(i + g.above, n);
+    const int32_t W = ST ? Wc : hi - lo + 1;
     if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + (i >> 4));
     const uint32_t pb = 8u * (pw & 3u);
     pw >>= 2;
@@ -396,7 +429,9 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
       }
     }
     // The sentinel right of the band (align.rs:2490-2494), after any rebase.
-    if (W < 32 * C) {
+    if constexpr (ST) {
+      if (sent) set_word16(h, f, ks, ms);
+    } else if (W < 32 * C) {
       if constexpr (kMasks) {
         if (W != Wm) set_masks(W);
 #pragma unroll
@@ -437,9 +472,21 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
   const int32_t endA = m < g.below ? m : g.below;
   const int64_t lastB = (int64_t)n + g.below;  // the last row whose band is not empty
   const int32_t endB = (int64_t)m < lastB ? m : (int32_t)lastB;
-  for (int32_t i = first; i <= endA && !stopped; ++i) stopped = row(i, std::false_type{});
-  for (int32_t i = max(endA + 1, first); i <= endB && !stopped; ++i)
-    stopped = row(i, std::true_type{});
+  const int32_t endS = min(endB, n - g.above);  // the last row with i + above <= n
+  for (int32_t i = first; i <= endA && !stopped; ++i)
+    stopped = row(i, std::integral_constant<int, 0>{});
+  int32_t i1 = max(endA + 1, first);
+  if (i1 <= endS) {
+    Wc = g.below + g.above + 1;
+    sent = Wc < 32 * C;
+    const int32_t Ls = Wc / C, c = Wc - Ls * C;
+    ks = c < C2 ? c : c - C2;
+    ms = lane == Ls ? (c < C2 ? 0xffffu : 0xffff0000u) : 0u;
+    Wm = -1;
+    for (; i1 <= endS && !stopped; ++i1) stopped = row(i1, std::integral_constant<int, 2>{});
+  }
+  for (int32_t i = i1; i <= endB && !stopped; ++i)
+    stopped = row(i, std::integral_constant<int, 1>{});
   if (!stopped && endB < m) {
     // Row endB + 1 lies past the text: the pass ends there with no score (align.rs:2543-2553).
     r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)(endB + 1),
