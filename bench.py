@@ -39,6 +39,20 @@ GOLD = {"c1": "myers-infix-10k", "c2": "affine-global-band128-cigar-20k",
         "c5": "serving-poisson-2000rps-bursts5x",
         "c2-score": "affine-global-band128-score-20k",
         "c3": "uneven-myers+affine-100k"}
+# Variants of a workload (--variant): the windowed read-end extension the mapper runs on the
+# config-2 pairs (align.rs:957-982; window x + 20 + x / 10, X-drop 50, end bonus 5,
+# map/src/lib.rs:2101, 235-239), and config 1 with each pair capped at its distance + 16.
+VARIANTS = {("c2", "window"): "affine-extend-window-band128-xdrop50",
+            ("c1", "kslack"): "myers-infix-10k-cap-d+16"}
+WINDOW = (20, 10, 50, 5)  # pad, pad_div, xdrop, end bonus
+K_SLACK = 16
+
+
+def workload_name(args) -> str:
+    if args.variant != "base":
+        name = VARIANTS[(args.config, args.variant)]
+        return name + ("-cigar" if args.config == "c2" and args.cigar else "")
+    return GOLD[args.config if args.cigar or args.config != "c2" else "c2-score"]
 OPS_PER_CELL = {"affine_tb": 12, "affine": 10, "myers": 0.625}
 
 
@@ -131,7 +145,7 @@ def make_jobs(B, pairs, kind, mode, want_cigar, band=None):
     return jobs
 
 
-def workload(cfg: str, scale: float, cigar: bool = True):
+def workload(cfg: str, scale: float, cigar: bool = True, variant: str = "base"):
     from spearfish_gb300 import batch as B
     from spearfish_gb300 import workloads as W
     if cfg == "c1":
@@ -139,6 +153,13 @@ def workload(cfg: str, scale: float, cigar: bool = True):
         return w.pool, make_jobs(B, w, B.JOB_MYERS, 0, False), [w], "myers"
     if cfg == "c2":
         w = W.config2(int(20_000 * scale))
+        if variant == "window":
+            pad, div, xdrop, bonus = WINDOW
+            jobs = make_jobs(B, w, B.JOB_EXTEND_WINDOW, 1, cigar)
+            jobs["window"] = jobs["m"].astype(np.uint64) + pad + jobs["m"] // div
+            jobs["xdrop"] = xdrop
+            jobs["end_bonus"] = bonus
+            return w.pool, jobs, [w], "affine_tb" if cigar else "affine"
         return w.pool, make_jobs(B, w, B.JOB_AFFINE, 2, cigar), [w], "affine_tb" if cigar else "affine"
     my, af = W.config3(int(100_000 * scale))
     # One pool: the affine pairs' offsets shift past the Myers pool.
@@ -213,13 +234,15 @@ def cells_of(jobs, results, B) -> int:
     return int(results["cells"].astype(np.uint64).sum())
 
 
-def cpu_baseline(cfg, pairs_list, seconds: float, threads: int):
-    """The reference's path restated in C (oracle), all host cores, bounded sample."""
+def cpu_baseline(cfg, pairs_list, seconds: float, threads: int, variant: str = "base",
+                 caps=None):
+    """The reference's path restated in C (oracle), all host cores, bounded sample.  caps:
+    per-pair Myers caps (the kslack variant)."""
     import oracle as O
     level = O.set_level(1)  # NEON rows where the host has them (the reference's level there)
     w = pairs_list[-1]
-    kind = 0 if cfg == "c1" else 1
-    mode = 0 if cfg == "c1" else 2
+    kind = 0 if cfg == "c1" else (2 if variant == "window" else 1)
+    mode = 0 if cfg == "c1" else (1 if variant == "window" else 2)
     band = None if cfg == "c1" else int(w.band[0]) if cfg == "c2" else None
     total_cells, total_t, done = 0, 0.0, 0
     idx = np.arange(len(w))
@@ -243,7 +266,9 @@ def cpu_baseline(cfg, pairs_list, seconds: float, threads: int):
             cells = c1 + c2
         else:
             _, cells = O.run_pairs(kind, threads, sub.pool, sub.p_off, sub.m, sub.pool, sub.t_off,
-                                   sub.n, mode, sc=O.ONT, band=band)
+                                   sub.n, mode, sc=O.ONT, band=band,
+                                   kv=None if caps is None else caps[sel],
+                                   extend=WINDOW if variant == "window" else None)
         total_t += time.perf_counter() - t0
         total_cells += cells
         done += len(sel)
@@ -256,16 +281,25 @@ def cpu_baseline(cfg, pairs_list, seconds: float, threads: int):
             "arch": platform.machine()}
 
 
+def kslack_caps(w, threads: int) -> np.ndarray:
+    """Per-pair caps of the kslack variant: each pair's distance + 16 (the oracle's
+    uncapped distances; the GPU's are the same, as the parity tests check)."""
+    import oracle as O
+    d, _ = O.run_pairs(0, threads, w.pool, w.p_off, w.m, w.pool, w.t_off, w.n, 0)
+    return (d.astype(np.int64) + K_SLACK).astype(np.uint32)
+
+
 def run_reference(args, ws, rank):
     """Reference arm: the CPU restatement on all host threads, rank 0 only."""
     if rank != 0:
         return
     import oracle as O
-    _, _, pairs_list, _ = workload(args.config, args.scale)
+    _, jobs, pairs_list, _ = workload(args.config, args.scale, True, args.variant)
     threads = O.host_threads()
+    caps = kslack_caps(pairs_list[-1], threads) if args.variant == "kslack" else None
     per_step = []
     for s in range(args.warmup + args.steps):
-        r = cpu_baseline(args.config, pairs_list, args.ref_seconds, threads)
+        r = cpu_baseline(args.config, pairs_list, args.ref_seconds, threads, args.variant, caps)
         if s >= args.warmup:
             per_step.append(r)
     v = statistics.mean(r["value"] for r in per_step)
@@ -273,7 +307,7 @@ def run_reference(args, ws, rank):
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": GOLD[args.config], "parallelism": "host threads"},
+            "config": {"workload": workload_name(args), "parallelism": "host threads"},
             "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
                              "sample": per_step[-1]["sample"], "level": per_step[-1]["level"]},
             "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,
@@ -397,9 +431,14 @@ def main():
     ap.add_argument("--plain-pairs", type=int, default=200)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cigar", type=int, default=1, help="c2/c3: traceback + CIGAR (1) or score only (0)")
+    ap.add_argument("--variant", default="base", choices=["base", "window", "kslack"],
+                    help="c2: window = the mapper's windowed read-end extension; "
+                         "c1: kslack = each pair capped at its distance + 16")
     ap.add_argument("--tune", type=int, default=None,
                     help="autotune the length buckets' kernel classes first (default: on)")
     args = ap.parse_args()
+    if args.variant != "base" and (args.config, args.variant) not in VARIANTS:
+        ap.error(f"--variant {args.variant} does not apply to {args.config}")
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -418,8 +457,19 @@ def main():
     build.build()
     lib = _abi.load()
     torch.cuda.set_device(local)
-    pool, jobs, pairs_list, kind = workload(args.config, args.scale, bool(args.cigar))
+    pool, jobs, pairs_list, kind = workload(args.config, args.scale, bool(args.cigar), args.variant)
     ctx = B.Context(local)
+    caps = None
+    if args.variant == "kslack":
+        # Untimed: each pair's distance from an uncapped run, then the cap d + 16.
+        pre = B.Plan(ctx, jobs, pool.size)
+        pre.upload(pool)
+        pre.execute()
+        pre.sync()
+        d = pre.download().results["distance"].astype(np.int64)
+        pre.close()
+        caps = (d + K_SLACK).astype(np.uint32)
+        jobs["k"] = caps
     plan = B.Plan(ctx, jobs, pool.size)
     plan.upload(pool)
     tune_report = None
@@ -566,6 +616,14 @@ def main():
         for q in range(n):
             if kind == "myers":
                 A.distance(w.pattern(q), w.text(q), A.Mode.Infix)
+            elif args.variant == "window":
+                win = int(jobs["window"][q])
+                if args.cigar:
+                    A.affine_extend_window_cigar(w.pattern(q), w.text(q), win, A.Affine.ONT,
+                                                 int(w.band[q]), WINDOW[3], WINDOW[2])
+                else:
+                    A.affine_extend_window(w.pattern(q), w.text(q), win, A.Affine.ONT,
+                                           int(w.band[q]), WINDOW[3], WINDOW[2])
             elif not args.cigar:
                 A.affine(w.pattern(q), w.text(q), A.Mode.Global, A.Affine.ONT, int(w.band[q]))
             else:
@@ -576,20 +634,23 @@ def main():
         pc = (c1 - c0) if kind != "myers" else int(
             sum(int(w.m[q]) * int(w.n[q]) for q in range(n)))
         plain = {"value": pc / dt / 1e9, "unit": "GCUPS", "pairs": n,
-                 "call": "sf_affine_cigar" if kind != "myers" else "sf_distance",
+                 "call": ("sf_distance" if kind == "myers" else
+                          ("sf_affine_extend_window" if args.variant == "window" else "sf_affine") +
+                          ("_cigar" if args.cigar else "")),
                  "ms_per_pair": dt / n * 1e3}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         import oracle as O
-        cpu = cpu_baseline(args.config, pairs_list, args.cpu_seconds, O.host_threads())
+        cpu = cpu_baseline(args.config, pairs_list, args.cpu_seconds, O.host_threads(),
+                           args.variant, caps)
 
     if rank == 0:
         line = {"metric": "alignment GCUPS", "value": value, "unit": "GCUPS", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "int32", "data": "synthetic (seeded; error model of sim.rs)",
-                "config": {"workload": GOLD[args.config if args.cigar or args.config != "c2" else "c2-score"],
+                "config": {"workload": workload_name(args),
                            "pairs": int(len(jobs)),
                            "cells_per_step": cells, "l2": "flushed (256 MB write) before each step",
                            "parallelism": f"replicas x{ws}", "form": "batched persistent plan, CUDA graph",

@@ -31,6 +31,11 @@ class Affine(C.Structure):
     _fields_ = [("mat", C.c_int32), ("mis", C.c_int32), ("open", C.c_int32), ("ext", C.c_int32)]
 
 
+class ExtendOpts(C.Structure):
+    _fields_ = [("pad", C.c_uint64), ("pad_div", C.c_uint64), ("xdrop", C.c_int32),
+                ("end_bonus", C.c_int32)]
+
+
 class Dp(C.Structure):
     _fields_ = [("score", C.c_int32), ("clip_best", C.c_int32), ("cut_best", C.c_int32),
                 ("cut_score", C.c_int32), ("score_col", C.c_uint64), ("clip_i", C.c_uint64),
@@ -112,8 +117,9 @@ def lib():
         L.or_get_level.argtypes = []
         L.or_run_pairs.restype = C.c_uint64
         L.or_run_pairs.argtypes = [C.c_int, C.c_int, _u8p, _u64p, _u64p, _u8p, _u64p, _u64p,
-                                   C.c_uint64, C.c_int, C.c_uint32, C.POINTER(Affine),
-                                   C.c_uint64, _i64p]
+                                   C.c_uint64, C.c_int, C.c_uint32, C.POINTER(C.c_uint32),
+                                   C.POINTER(Affine), C.c_uint64, C.POINTER(ExtendOpts),
+                                   _i64p]
         _lib = L
     return _lib
 
@@ -300,17 +306,24 @@ def set_level(level: int) -> int:
 
 
 def run_pairs(kind: int, threads: int, pseq, poff, plen, tseq, toff, tlen, mode: int,
-              k: int = 0xFFFFFFFF, sc=ONT, band=None) -> tuple[np.ndarray, int]:
-    """All pairs on `threads` host threads; returns (per-pair result, cells)."""
+              k: int = 0xFFFFFFFF, sc=ONT, band=None, kv=None,
+              extend: Optional[tuple] = None) -> tuple[np.ndarray, int]:
+    """All pairs on `threads` host threads; returns (per-pair result, cells).  kind 0:
+    Myers (cap k, or per pair kv); 1: affine; 2: extend window, extend = (pad, pad_div,
+    xdrop, end_bonus)."""
     count = len(plen)
     out = np.zeros(count, dtype=np.int64)
     arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
             ((pseq, np.uint8), (poff, np.uint64), (plen, np.uint64), (tseq, np.uint8),
              (toff, np.uint64), (tlen, np.uint64))]
+    kva = None if kv is None else np.ascontiguousarray(kv, dtype=np.uint32)
+    ext = ExtendOpts(*extend) if extend is not None else None
     cells = lib().or_run_pairs(kind, threads, _p(arrs[0]), _p(arrs[1], _u64p),
                                _p(arrs[2], _u64p), _p(arrs[3]), _p(arrs[4], _u64p),
-                               _p(arrs[5], _u64p), count, mode, k, C.byref(_sc(sc)),
-                               _band(band), _p(out, _i64p))
+                               _p(arrs[5], _u64p), count, mode, k,
+                               None if kva is None else _p(kva, C.POINTER(C.c_uint32)),
+                               C.byref(_sc(sc)), _band(band),
+                               None if ext is None else C.byref(ext), _p(out, _i64p))
     return out, int(cells)
 
 

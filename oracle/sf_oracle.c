@@ -1093,10 +1093,12 @@ int64_t or_cigar_score(const uint8_t *p, uint64_t m, const uint8_t *t, uint64_t 
 typedef struct {
     int kind, mode;
     uint32_t k;
+    const uint32_t *kv;
     const uint8_t *pseq, *tseq;
     const uint64_t *poff, *plen, *toff, *tlen;
     uint64_t count, band;
     const or_affine_t *sc;
+    or_extend_opts_t ext;
     int64_t *out;
     _Atomic uint64_t next;
     _Atomic uint64_t cells;
@@ -1112,8 +1114,18 @@ static void *pair_worker(void *arg) {
         const uint8_t *p = j->pseq + j->poff[q], *t = j->tseq + j->toff[q];
         uint64_t m = j->plen[q], n = j->tlen[q];
         if (j->kind == 0) {
-            j->out[q] = or_myers_distance(p, m, t, n, j->mode, j->k);
+            j->out[q] = or_myers_distance(p, m, t, n, j->mode, j->kv ? j->kv[q] : j->k);
             cells += m * n;
+        } else if (j->kind == 2) {
+            /* align.rs:957-982 `affine_extend_window` with the mapper's window
+             * x + pad + x / pad_div (map/src/lib.rs:2101). */
+            const uint64_t w = m + j->ext.pad + (j->ext.pad_div ? m / j->ext.pad_div : 0);
+            or_dp_t d;
+            run_core(p, m, t, n, OR_PREFIX, j->sc, j->band, umax(w, n), 1, j->ext.xdrop, 1,
+                     OR_NOLIMIT, &d, NULL, j->level);
+            const int32_t whole = sat_add32(d.score, j->ext.end_bonus);
+            j->out[q] = d.clip_best >= whole ? d.clip_best : whole;
+            cells += d.cells;
         } else {
             or_dp_t d;
             run_core(p, m, t, n, j->mode, j->sc, j->band, n, 0, 0, 0, OR_NOLIMIT, &d, NULL,
@@ -1129,10 +1141,12 @@ static void *pair_worker(void *arg) {
 uint64_t or_run_pairs(int kind, int threads, const uint8_t *pseq, const uint64_t *poff,
                       const uint64_t *plen, const uint8_t *tseq, const uint64_t *toff,
                       const uint64_t *tlen, uint64_t count, int mode, uint32_t k,
-                      const or_affine_t *sc, uint64_t band, int64_t *out) {
-    pair_job job = {.kind = kind, .mode = mode, .k = k, .pseq = pseq, .tseq = tseq,
+                      const uint32_t *kv, const or_affine_t *sc, uint64_t band,
+                      const or_extend_opts_t *ext, int64_t *out) {
+    pair_job job = {.kind = kind, .mode = mode, .k = k, .kv = kv, .pseq = pseq, .tseq = tseq,
                     .poff = poff, .plen = plen, .toff = toff, .tlen = tlen, .count = count,
                     .band = band, .sc = sc, .out = out, .level = atomic_load(&g_level)};
+    if (ext) job.ext = *ext;
     atomic_store(&job.next, 0);
     atomic_store(&job.cells, 0);
     if (threads < 1) threads = 1;

@@ -151,16 +151,24 @@ int64_t or_cigar_score(const uint8_t *p, uint64_t m, const uint8_t *t,
 int or_set_level(int level);
 int or_get_level(void);
 
-/* Jobs: Myers distance per pair (kind 0) or `affine` per pair (kind 1).
- * Sequences are byte codes; pair q is p[poff[q]..+plen[q]] vs
- * t[toff[q]..+tlen[q]].  out: int64 per pair.  Returns the summed
- * DP_WORK cells (affine) or m*n cells (Myers). */
+/* Extension jobs (kind 2): the window x + pad + x / pad_div (pad_div 0: no
+ * term) for a read end of x bases, X-drop and end bonus. */
+typedef struct {
+    uint64_t pad, pad_div;
+    int32_t xdrop, end_bonus;
+} or_extend_opts_t;
+
+/* Jobs: Myers distance per pair (kind 0; cap kv[q] when kv is not NULL, else
+ * k), `affine` per pair (kind 1) or `affine_extend_window` per pair (kind 2,
+ * whole score).  Sequences are byte codes; pair q is p[poff[q]..+plen[q]] vs
+ * t[toff[q]..+tlen[q]].  out: int64 per pair.  Returns the summed DP_WORK
+ * cells (affine) or m*n cells (Myers). */
 uint64_t or_run_pairs(int kind, int threads, const uint8_t *pseq,
                       const uint64_t *poff, const uint64_t *plen,
                       const uint8_t *tseq, const uint64_t *toff,
                       const uint64_t *tlen, uint64_t count, int mode,
-                      uint32_t k, const or_affine_t *sc, uint64_t band,
-                      int64_t *out);
+                      uint32_t k, const uint32_t *kv, const or_affine_t *sc,
+                      uint64_t band, const or_extend_opts_t *ext, int64_t *out);
 
 #ifdef __cplusplus
 }

@@ -212,3 +212,15 @@ def test_run_pairs_matches_single():
     out, cells = O.run_pairs(1, 3, pc, po, pl, tc, to, tl, R.GLOBAL, sc=R.ONT, band=16)
     assert [int(x) for x in out] == [O.affine(p, t, R.GLOBAL, R.ONT, 16) for p, t in zip(ps, ts)]
     assert cells == sum(O.affine_dp(p, t, R.GLOBAL, R.ONT, 16)["cells"] for p, t in zip(ps, ts))
+    # Per-pair caps (Myers) and windowed extensions (the window rule x + 20 + x / 10).
+    kv = rng.integers(0, 200, len(ps)).astype(np.uint32)
+    out, _ = O.run_pairs(0, 2, pc, po, pl, tc, to, tl, R.PREFIX, kv=kv)
+    want = [O.myers_distance(p, t, R.PREFIX, int(k)) for p, t, k in zip(ps, ts, kv)]
+    assert [None if int(x) < 0 else int(x) for x in out] == want
+    out, cells = O.run_pairs(2, 3, pc, po, pl, tc, to, tl, R.PREFIX, sc=R.ONT, band=16,
+                             extend=(20, 10, 50, 5))
+    win = [len(p) + 20 + len(p) // 10 for p in ps]
+    assert [int(x) for x in out] == [O.affine_extend_window(p, t, w, R.ONT, 16, 5, 50)[0]
+                                     for p, t, w in zip(ps, ts, win)]
+    assert cells == sum(O.affine_dp(p, t, R.PREFIX, R.ONT, 16, geom=max(w, len(t)),
+                                    clip=(50, True))["cells"] for p, t, w in zip(ps, ts, win))
