@@ -11,6 +11,7 @@
 // its tests `random_vs_naive` / `related_vs_naive`), so comparing the full-column distance
 // with k gives the same Option<u32>.
 #include <type_traits>
+#include <utility>
 
 #include "sf_internal.cuh"
 
@@ -29,22 +30,39 @@ __device__ __forceinline__ uint32_t match16(uint32_t w, uint32_t c) {
   return y;
 }
 
-// align.rs:50-66 `block`, with the output row given as a one-bit mask.
-__device__ __forceinline__ int myers_step(uint64_t& pv, uint64_t& mv, uint64_t eq, int hin,
-                                          uint64_t outbit) {
-  const uint64_t neg = (uint64_t)(hin < 0), pos = (uint64_t)(hin > 0);
+// Calls f(std::integral_constant<int, k>{}) for k = 0 .. 15.
+template <class F, int... K>
+__device__ __forceinline__ void sf_unroll16_impl(F&& f, std::integer_sequence<int, K...>) {
+  (f(std::integral_constant<int, K>{}), ...);
+}
+template <class F>
+__device__ __forceinline__ void sf_unroll16(F&& f) {
+  sf_unroll16_impl(f, std::make_integer_sequence<int, 16>{});
+}
+
+// align.rs:50-66 `block`.  The horizontal delta entering and leaving the block travels as
+// two bits (pos: +1, neg: -1); the delta leaving is read at the block's last row `ob`
+// (63, or the pattern's last row in its last block), as bit 0 of
+// funnelshift_rc(lo, hi, ob) >> sub with sub = max(ob - 32, 0).
+__device__ __forceinline__ void myers_step(uint64_t& pv, uint64_t& mv, uint64_t eq,
+                                           uint32_t& pos, uint32_t& neg, uint32_t ob,
+                                           uint32_t sub) {
   const uint64_t p = pv, m = mv;
   const uint64_t xv = eq | m;
   eq |= neg;
   const uint64_t xh = (((eq & p) + p) ^ p) | eq;
   uint64_t ph = m | ~(xh | p);
   uint64_t mh = p & xh;
-  const int hout = (int)((ph & outbit) != 0) - (int)((mh & outbit) != 0);
+  const uint32_t po =
+      (__funnelshift_rc((uint32_t)ph, (uint32_t)(ph >> 32), ob) >> sub) & 1u;
+  const uint32_t no =
+      (__funnelshift_rc((uint32_t)mh, (uint32_t)(mh >> 32), ob) >> sub) & 1u;
   ph = (ph << 1) | pos;
   mh = (mh << 1) | neg;
   pv = mh | ~(xv | ph);
   mv = ph & xv;
-  return hout;
+  pos = po;
+  neg = no;
 }
 
 template <int B>
@@ -75,37 +93,53 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     const uint32_t last_block = blocks ? blocks - 1 : 0;
     const uint32_t last_bit = m ? (m - 1) % 64 : 0;
 
-    // Match masks of this lane's blocks (align.rs:75-84).
-    uint64_t peq[SMEM ? 1 : B][4];
-    uint64_t pv[B], mv[B], outbit[B];
+    // Match masks of this lane's blocks (align.rs:75-84): in shared memory per code for wide
+    // lanes; in registers as the pattern's two bit planes otherwise, eq(c) = bits whose code
+    // equals c.  Bits past the pattern's last row (and blocks past it) hold codes too: the
+    // row recurrences only move information to higher rows, so they never reach the rows the
+    // distance is read at.
+    uint64_t pl0[SMEM ? 1 : B], pl1[SMEM ? 1 : B];
+    uint64_t pv[B], mv[B];
+    uint32_t ob[B], osub[B];
 #pragma unroll
     for (int bb = 0; bb < B; ++bb) {
       const uint32_t b = (uint32_t)l * B + bb;
-      uint64_t q[4] = {0, 0, 0, 0};
+      uint64_t q[4] = {0, 0, 0, 0}, b0 = 0, b1 = 0;
       if (has && b < blocks) {
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
           const uint64_t wi = J.p_word + (uint64_t)b * 4 + h;
           const uint32_t w = __funnelshift_r(__ldg(a.pool + wi), __ldg(a.pool + wi + 1), 2);
+          if constexpr (SMEM) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) q[c] |= (uint64_t)match16(w, (uint32_t)c) << (16 * h);
-        }
-        if (b == last_block && last_bit < 63) {
-          const uint64_t keep = (1ull << (last_bit + 1)) - 1;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) q[c] &= keep;
+            for (int c = 0; c < 4; ++c) q[c] |= (uint64_t)match16(w, (uint32_t)c) << (16 * h);
+          } else {
+            // Gather the 16 codes' low and high bits.
+            uint32_t lo = w & 0x55555555u, hi = (w >> 1) & 0x55555555u;
+            lo = (lo | (lo >> 1)) & 0x33333333u;
+            lo = (lo | (lo >> 2)) & 0x0F0F0F0Fu;
+            lo = (lo | (lo >> 4)) & 0x00FF00FFu;
+            lo = (lo | (lo >> 8)) & 0x0000FFFFu;
+            hi = (hi | (hi >> 1)) & 0x33333333u;
+            hi = (hi | (hi >> 2)) & 0x0F0F0F0Fu;
+            hi = (hi | (hi >> 4)) & 0x00FF00FFu;
+            hi = (hi | (hi >> 8)) & 0x0000FFFFu;
+            b0 |= (uint64_t)lo << (16 * h);
+            b1 |= (uint64_t)hi << (16 * h);
+          }
         }
       }
+      if constexpr (SMEM) {
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        if constexpr (SMEM)
-          speq[((size_t)bb * 4 + c) * 32 + lane] = q[c];
-        else
-          peq[bb][c] = q[c];
+        for (int c = 0; c < 4; ++c) speq[((size_t)bb * 4 + c) * 32 + lane] = q[c];
+      } else {
+        pl0[bb] = b0;
+        pl1[bb] = b1;
       }
       pv[bb] = ~0ull;
       mv[bb] = 0;
-      outbit[bb] = 1ull << (b == last_block ? last_bit : 63);
+      ob[bb] = b == last_block ? last_bit : 63u;
+      osub[bb] = ob[bb] >= 32 ? ob[bb] - 32 : 0u;
     }
     if constexpr (SMEM) __syncwarp();
 
@@ -115,24 +149,38 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     int score = (int)m, best = (int)m;
     int steps = has && m > 0 ? (int)n + P - 1 : 0;
     steps = __reduce_max_sync(FULL, steps);
-    uint32_t payload = 0;  // (text code << 2) | (h + 1)
+    uint32_t payload = 0;  // (text code << 2) | (pos << 1) | neg
     uint32_t tw = 0;       // the text word holding base t + 1 (used by lane 0)
     const bool glob = J.mode == 2;
     // One step of the pipeline.  Lanes keep their state only while they are past the fill
     // (FILL: some lanes have not reached column 0 yet); past its text's end a lane computes
     // on state nothing reads any more, so the steady loop needs no masking and no branches.
-    auto step = [&](int t, auto fill) {
+    // K < 0: the step reads its text base itself; K = 0..15: the step is the K-th of a run of
+    // 16 whose bases all sit in `tw`, loaded before the run.  Every lane keeps a running
+    // score (only the owner's is used): the column's distance while the lane's column lies in
+    // the text, and the least of them (Infix, Prefix; Global takes the last).
+    const int jend = (int)n + l;  // steps t < jend have this lane's column j = t - l < n
+    auto step = [&](int t, auto fill, auto kk) {
       constexpr bool FILL = decltype(fill)::value;
+      constexpr int K = decltype(kk)::value;
       const int j = t - l;
-      const bool live = has && m > 0 && j >= 0 && j < (int)n;
+      const bool live = FILL ? (j >= 0 && t < jend) : t < jend;
       const uint32_t in = __shfl_up_sync(FULL, payload, 1, P);
-      // A new text word every 16 steps, read only while it lies inside this text (base t + 1
-      // of a text of n bases sits in word (t + 1) / 16 after the leading pad base).
-      if ((((t + 1) & 15) == 0 || t == 0) && (uint32_t)(t + 1) <= n)
-        tw = __ldg(a.pool + J.t_word + ((uint32_t)(t + 1) >> 4));
-      const uint32_t c0 = (tw >> (2 * ((t + 1) & 15))) & 3u;
+      uint32_t c0;
+      if constexpr (K < 0) {
+        // A new text word every 16 steps, read only while it lies inside this text (base
+        // t + 1 of a text of n bases sits in word (t + 1) / 16 after the leading pad base).
+        if ((((t + 1) & 15) == 0 || t == 0) && (uint32_t)(t + 1) <= n)
+          tw = __ldg(a.pool + J.t_word + ((uint32_t)(t + 1) >> 4));
+        c0 = (tw >> (2 * ((t + 1) & 15))) & 3u;
+      } else {
+        c0 = (tw >> (2 * K)) & 3u;
+      }
       const uint32_t c = l == 0 ? c0 : (in >> 2);
-      int h = l == 0 ? top : (int)(in & 3) - 1;
+      uint32_t pos = l == 0 ? (uint32_t)top : (in >> 1) & 1u;
+      uint32_t neg = l == 0 ? 0u : in & 1u;
+      // eq(c) from the bit planes: both code bits equal c's.
+      const uint64_t m0 = (c & 1u) ? ~0ull : 0ull, m1 = (c & 2u) ? ~0ull : 0ull;
       int hlast = 0;
 #pragma unroll
       for (int bb = 0; bb < B; ++bb) {
@@ -140,28 +188,38 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
         if constexpr (SMEM)
           eq = speq[((size_t)bb * 4 + c) * 32 + lane];
         else
-          eq = c == 0 ? peq[bb][0] : c == 1 ? peq[bb][1] : c == 2 ? peq[bb][2] : peq[bb][3];
+          eq = ~(pl0[bb] ^ m0) & ~(pl1[bb] ^ m1);
         if constexpr (FILL) {
           uint64_t p2 = pv[bb], m2 = mv[bb];
-          h = myers_step(p2, m2, eq, h, outbit[bb]);
+          myers_step(p2, m2, eq, pos, neg, ob[bb], osub[bb]);
           if (j >= 0) {
             pv[bb] = p2;
             mv[bb] = m2;
           }
         } else {
-          h = myers_step(pv[bb], mv[bb], eq, h, outbit[bb]);
+          myers_step(pv[bb], mv[bb], eq, pos, neg, ob[bb], osub[bb]);
         }
-        hlast = bb == own_bb ? h : hlast;
+        hlast = bb == own_bb ? (int)pos - (int)neg : hlast;
       }
-      const bool upd = owner && live;
-      score = upd ? score + hlast : score;
-      best = upd ? (glob ? (j + 1 == (int)n ? score : best) : min(best, score)) : best;
-      payload = (c << 2) | (uint32_t)(h + 1);
+      score += live ? hlast : 0;
+      best = min(best, score);
+      payload = (c << 2) | (pos << 1) | neg;
     };
+    using kAny = std::integral_constant<int, -1>;
     const int fill = steps < P - 1 ? steps : P - 1;
     int t = 0;
-    for (; t < fill; ++t) step(t, std::true_type{});
-    for (; t < steps; ++t) step(t, std::false_type{});
+    for (; t < fill; ++t) step(t, std::true_type{}, kAny{});
+    // Steady steps: with register blocks, single ones up to a text-word boundary, then runs of
+    // 16 with one load each (wider lanes keep the loop short: their step is long already).
+    if constexpr (!SMEM) {
+      for (; t < steps && ((t + 1) & 15) != 0; ++t) step(t, std::false_type{}, kAny{});
+      for (; t + 16 <= steps; t += 16) {
+        if ((uint32_t)(t + 1) <= n) tw = __ldg(a.pool + J.t_word + ((uint32_t)(t + 1) >> 4));
+        sf_unroll16([&](auto kt) { step(t + decltype(kt)::value, std::false_type{}, kt); });
+      }
+    }
+    for (; t < steps; ++t) step(t, std::false_type{}, kAny{});
+    if (glob) best = score;
     if (has) {
       if (m == 0) {
         if (l == 0) {
