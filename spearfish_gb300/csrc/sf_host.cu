@@ -222,9 +222,11 @@ int plan_build(sf_plan* P) {
     keys.push_back({p.p_off, p.m, (uint32_t)(2 * q)});
     keys.push_back({p.t_off, p.n, (uint32_t)(2 * q + 1)});
   }
-  std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+  // In offset order: a pool built in job order (the usual case) needs no sort.
+  auto key_less = [](const Key& a, const Key& b) {
     return a.off != b.off ? a.off < b.off : a.len < b.len;
-  });
+  };
+  if (!std::is_sorted(keys.begin(), keys.end(), key_less)) std::sort(keys.begin(), keys.end(), key_less);
   std::vector<uint64_t> word_of(2 * np);
   P->seq_boff.clear();
   P->seq_len.clear();
@@ -325,6 +327,24 @@ int plan_build(sf_plan* P) {
       q += cnt;
     }
   }
+  // The tune table's answers, memoised per class (a batch has few classes).
+  struct TuneMemo {
+    ClassKey key;
+    int c, lanes;
+  };
+  std::vector<TuneMemo> memo;
+  auto tuned = [&](int kind, int& c, bool wide, bool tb, int& lanes) {
+    if (!tune || tune->empty()) return;
+    const ClassKey k{kind, c, wide ? 1 : 0, tb ? 1 : 0, lanes};
+    for (size_t u = memo.size(); u-- > 0;)
+      if (memo[u].key == k) {
+        c = memo[u].c;
+        lanes = memo[u].lanes;
+        return;
+      }
+    apply_tune(tune, kind, c, wide, tb, lanes);
+    memo.push_back(TuneMemo{k, c, lanes});
+  };
   std::vector<uint64_t> pass_work(np, 0);
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (size_t q = 0; q < np; ++q) {
@@ -333,7 +353,7 @@ int plan_build(sf_plan* P) {
       int b = 1, lanes = 1;
       int rc = choose_myers_class(p.m, b, lanes);
       if (rc) return rc;
-      apply_tune(tune, PK_MYERS, b, false, false, lanes);
+      tuned(PK_MYERS, b, false, false, lanes);
       MJob m{};
       m.p_word = word_of[2 * q];
       m.t_word = word_of[2 * q + 1];
@@ -358,7 +378,7 @@ int plan_build(sf_plan* P) {
     int ln = 32;
     classify_affine(p, flags, wmax, use16, kind, c, wide, ln, lanes16);
     const bool tb = p.want_cigar && p.kind != PK_LOCAL;
-    if (!wide) apply_tune(tune, kind, c, false, tb, ln);
+    if (!wide) tuned(kind, c, false, tb, ln);
     if (tb) {
       flags |= F_TB;
       j.tb_word = tb_words;
@@ -486,11 +506,25 @@ int plan_build(sf_plan* P) {
   std::vector<uint64_t> bw(keys2.size());
   for (size_t u = 0; u < keys2.size(); ++u) bw[rank[u]] = bwork[u];
   bwork.swap(bw);
+  // Longest first within a bucket, by work rounded to 1/16 of its power of two (a stable
+  // counting sort: equal rounded work keeps job order).
+  auto wbin = [](uint64_t w) -> uint32_t {
+    if (w < 16) return (uint32_t)w;
+    const int e = 63 - __builtin_clzll(w);  // w in [2^e, 2^(e+1))
+    return (uint32_t)(16 * (e - 3) + ((w >> (e - 4)) & 15));
+  };
+  constexpr uint32_t kBins = 16 * 61 + 16;
+  std::vector<uint32_t> bin_at(kBins + 1);
+  std::vector<std::pair<uint64_t, uint32_t>> tmp;
   for (size_t u = 0; u < sorted_keys.size(); ++u) {
     auto b0 = byb.begin() + (ptrdiff_t)start[u], b1 = byb.begin() + (ptrdiff_t)start[u + 1];
-    std::sort(b0, b1, [](const auto& a, const auto& b) {
-      return a.first != b.first ? a.first > b.first : a.second < b.second;
-    });
+    {
+      std::fill(bin_at.begin(), bin_at.end(), 0u);
+      for (auto it = b0; it != b1; ++it) bin_at[kBins - 1 - wbin(it->first) + 1]++;
+      for (uint32_t k = 0; k < kBins; ++k) bin_at[k + 1] += bin_at[k];
+      tmp.assign(b0, b1);
+      for (const auto& e : tmp) *(b0 + bin_at[kBins - 1 - wbin(e.first)]++) = e;
+    }
     Bucket b;
     b.kind = (PassKind)sorted_keys[u].kind;
     b.c = sorted_keys[u].c;
@@ -1915,8 +1949,11 @@ int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, cons
   int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes, ctx->store);
   if (rc) return rc;
   P->pool_bytes = pool_bytes;
-  if ((rc = plan_build(P))) return rc;
+  // The pool's copy runs while the host builds the plan.
+  CK(cudaSetDevice(ctx->dev));
+  if ((rc = P->d_bytes.ensure(std::max<uint64_t>(pool_bytes, 16)))) return rc;
   if ((rc = plan_upload_from(P, pool))) return rc;
+  if ((rc = plan_build(P))) return rc;
   if ((rc = plan_execute(P, false))) return rc;
   return sf_plan_download(P, results, ops, ops_cap, ops_used);
 }
