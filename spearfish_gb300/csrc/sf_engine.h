@@ -155,6 +155,7 @@ struct Bucket {
   int grid = 0, block = 128;
   uint64_t scratch_off = 0;       // wide rows: this bucket's slice of the scratch (int32s)
   uint64_t work = 0;              // estimated work (cells of its passes' widest rows)
+  uint64_t lat = 0;               // its longest pass's time, roughly (launch order)
   int stream = 0;                 // auxiliary stream it runs on
 };
 

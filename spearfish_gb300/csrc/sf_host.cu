@@ -258,6 +258,7 @@ int plan_build(sf_plan* P) {
   struct Item {
     uint32_t slot;
     uint64_t work;
+    uint64_t lat = 0;  // its warp's time, roughly: rows (steps) x the class's work per row
   };
   struct Key2 {
     int kind, c, wide, tb, lanes;
@@ -345,7 +346,7 @@ int plan_build(sf_plan* P) {
     apply_tune(tune, kind, c, wide, tb, lanes);
     memo.push_back(TuneMemo{k, c, lanes});
   };
-  std::vector<uint64_t> pass_work(np, 0);
+  std::vector<uint64_t> pass_work(np, 0), pass_lat(np, 0);
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
@@ -362,7 +363,9 @@ int plan_build(sf_plan* P) {
       m.mode = p.mode;
       m.k = p.k;
       P->slot[q] = (uint32_t)mj.size();
-      items.push_back({Key2{PK_MYERS, b, 0, 0, lanes}, Item{(uint32_t)mj.size(), (uint64_t)p.n}});
+      items.push_back({Key2{PK_MYERS, b, 0, 0, lanes},
+                       Item{(uint32_t)mj.size(), (uint64_t)p.n,
+                            ((uint64_t)p.n + (uint64_t)lanes) * (4u * (uint64_t)b + 4u)}});
       mj.push_back(m);
       continue;
     }
@@ -408,7 +411,10 @@ int plan_build(sf_plan* P) {
     P->slot[q] = (uint32_t)dj.size();
     const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
     pass_work[q] = work;
-    if (!P->chained[q]) items.push_back({Key2{kind, c, wide, tb, ln}, Item{(uint32_t)dj.size(), work}});
+    const uint64_t row_cost = (uint64_t)c * (wide ? (uint64_t)wide_chunks(c, wmax) : 1u) + 8u;
+    pass_lat[q] = (uint64_t)std::max<uint32_t>(p.m, 1) * row_cost;
+    if (!P->chained[q])
+      items.push_back({Key2{kind, c, wide, tb, ln}, Item{(uint32_t)dj.size(), work, pass_lat[q]}});
     dj.push_back(j);
     dp.push_back(pr);
     tj.push_back(t);
@@ -430,10 +436,11 @@ int plan_build(sf_plan* P) {
     ch.want = (uint32_t)want.size();
     ch.snap_word = snap_words;
     std::vector<uint32_t> rows;
-    uint64_t work = 0;
+    uint64_t work = 0, lat = 0;
     for (size_t u = sb.first; u < sb.first + sb.count; ++u) {
       if (u > sb.first) rows.push_back(P->passes[u].resume);
       work += pass_work[u];
+      lat += pass_lat[u];
     }
     std::sort(rows.begin(), rows.end());
     rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
@@ -448,7 +455,7 @@ int plan_build(sf_plan* P) {
     }
     want.insert(want.end(), rows.begin(), rows.end());
     snap_words += rows.size() * snap_slot_words(sb.c / 2);
-    items.push_back({Key2{PK_CHAIN16, sb.c, 0, 0, 32}, Item{(uint32_t)chains.size(), work}});
+    items.push_back({Key2{PK_CHAIN16, sb.c, 0, 0, 32}, Item{(uint32_t)chains.size(), work, lat}});
     chains.push_back(ch);
     n_chained += sb.count;
   }
@@ -534,9 +541,16 @@ int plan_build(sf_plan* P) {
     b.first = (uint32_t)start[u];
     b.count = (uint32_t)(start[u + 1] - start[u]);
     b.work = bwork[u];
+    for (auto it = b0; it != b1; ++it) {
+      order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
+      b.lat = std::max(b.lat, items[it->second].second.lat);
+    }
     P->buckets.push_back(b);
-    for (auto it = b0; it != b1; ++it) order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
   }
+  // Launch order: the buckets whose longest pass takes longest first, so that a few long
+  // passes (a small grid) run beside the bulk instead of after it.
+  std::stable_sort(P->buckets.begin(), P->buckets.end(),
+                   [](const Bucket& x, const Bucket& y) { return x.lat > y.lat; });
   // Launch shapes: persistent grids, at most what fits the device at once.  Wide buckets
   // may run concurrently (fan-out streams), so each gets its own scratch slice.
   int wide_warps = 0;
@@ -562,7 +576,7 @@ int plan_build(sf_plan* P) {
     }
   }
   P->wide_warps = wide_warps;
-  // Streams: round robin over the buckets in key order, so that their tails overlap.
+  // Streams: round robin over the buckets in launch order, so that their tails overlap.
   for (size_t u = 0; u < P->buckets.size(); ++u) P->buckets[u].stream = (int)(u % sf_context::kAux);
   // Device buffers.
   int rc;
@@ -649,7 +663,7 @@ int plan_build(sf_plan* P) {
                                          : "affine",
                   b.c,
                   b.wide ? "true" : "false", b.tb ? "true" : "false", b.lanes, b.count, b.grid,
-                  b.block, (unsigned long long)bwork[q]);
+                  b.block, (unsigned long long)b.work);
     d += buf;
   }
   d += "], \"chains\": " + std::to_string(P->n_chains) +
