@@ -224,7 +224,7 @@ struct sf_context {
   int dev = 0;
   int sms = 0;
   cudaStream_t s = nullptr;
-  static constexpr int kAux = 4;
+  static constexpr int kAux = 8;
   cudaStream_t aux[kAux] = {};
   cudaEvent_t fork = nullptr, join[kAux] = {};
   std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
