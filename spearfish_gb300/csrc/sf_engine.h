@@ -162,6 +162,9 @@ struct Bucket {
 }  // namespace sfe
 
 struct sf_store;
+namespace sfe {
+struct BuildScratch;
+}
 
 struct sf_plan {
   using Pass = sfe::Pass;
@@ -199,7 +202,11 @@ struct sf_plan {
   const sf_store* store = nullptr;
   // Class overrides for this plan only (the autotuner's trial plans); else the context's.
   const sfe::TuneTable* tune_override = nullptr;
-  // Out of line (sf_host.cu): deleting an owned context needs sf_context complete.
+  // Host-side build arrays kept between builds (sf_host.cu).
+  std::unique_ptr<sfe::BuildScratch> scratch;
+  // Out of line (sf_host.cu): deleting an owned context needs sf_context complete, and the
+  // build arrays their type.
+  sf_plan();
   ~sf_plan();
 };
 

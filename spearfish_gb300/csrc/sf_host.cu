@@ -11,6 +11,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 #include <vector>
@@ -189,6 +190,43 @@ DJob make_djob(const Pass& p, uint32_t& flags) {
 
 }  // namespace sfe
 
+namespace sfe {
+
+// A bucket's key (kernel class) and one work item of it.
+struct BucketKey {
+  int kind, c, wide, tb, lanes;
+  bool operator<(const BucketKey& o) const {
+    return std::tie(kind, c, wide, tb, lanes) < std::tie(o.kind, o.c, o.wide, o.tb, o.lanes);
+  }
+  bool operator==(const BucketKey& o) const {
+    return kind == o.kind && c == o.c && wide == o.wide && tb == o.tb && lanes == o.lanes;
+  }
+};
+struct BucketItem {
+  uint32_t slot;
+  uint64_t work;
+  uint64_t lat = 0;  // its warp's time, roughly: rows (steps) x the class's work per row
+};
+
+// A plan's host-side build arrays, kept between builds: a rebuild of a similar batch reuses
+// their memory instead of faulting in fresh pages.
+struct BuildScratch {
+  std::vector<uint64_t> word_of, pass_work, pass_lat, tb_need, ops_need;
+  std::vector<DJob> dj;
+  std::vector<DParams> dp;
+  std::vector<TJob> tj;
+  std::vector<uint16_t> cls;
+  std::vector<MJob> mj;
+  std::vector<uint32_t> wlist, kid, order;
+  std::vector<std::pair<BucketKey, BucketItem>> items, per;
+  std::vector<uint8_t> has_item, seq_table;
+  std::vector<std::pair<uint64_t, uint32_t>> byb, tmp;
+};
+
+}  // namespace sfe
+
+sf_plan::sf_plan() = default;
+
 sf_plan::~sf_plan() {
   if (graph) cudaGraphExecDestroy(graph);
   if (owns_ctx) delete ctx;
@@ -198,8 +236,37 @@ namespace sfe {
 
 uint64_t seq_words(uint64_t len) { return (len + 1 + 15) / 16; }
 
+// f(begin, end, worker) over [0, n) in contiguous chunks: on up to max_threads host threads
+// when every thread gets at least min_per_thread items, else (or when threads cannot be
+// started) on the calling thread alone.
+template <class F>
+void parallel_chunks(size_t n, size_t min_per_thread, int max_threads, F&& f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  size_t t = std::min<size_t>({(size_t)(hw ? hw : 1), (size_t)max_threads,
+                               min_per_thread ? n / min_per_thread : 1});
+  if (t <= 1) {
+    f(size_t(0), n, 0);
+    return;
+  }
+  const size_t chunk = (n + t - 1) / t;
+  std::vector<std::thread> th;
+  try {
+    for (size_t k = 1; k < t; ++k)
+      th.emplace_back([&f, k, chunk, n] { f(k * chunk, std::min(n, (k + 1) * chunk), (int)k); });
+  } catch (...) {
+    // Run the chunks no thread took here.
+    for (size_t k = th.size() + 1; k < t; ++k) f(k * chunk, std::min(n, (k + 1) * chunk), 0);
+  }
+  f(size_t(0), std::min(n, chunk), 0);
+  for (auto& x : th) x.join();
+}
+
 // Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
 int plan_build(sf_plan* P) {
+  using Key2 = BucketKey;
+  using Item = BucketItem;
+  if (!P->scratch) P->scratch.reset(new BuildScratch);
+  BuildScratch& S = *P->scratch;
   sf_context* ctx = P->ctx;
   CK(cudaSetDevice(ctx->dev));
   const size_t np = P->passes.size();
@@ -210,66 +277,91 @@ int plan_build(sf_plan* P) {
     uint32_t len;
     uint32_t idx;
   };
-  std::vector<Key> keys;
-  keys.reserve(2 * np);
-  for (size_t q = 0; q < np; ++q) {
-    const Pass& p = P->passes[q];
-    if ((p.p_off & kOffMask) + p.m > P->pool_bytes ||
-        (!(p.t_off & kStoreFlag) && (p.t_off & kOffMask) + p.n > P->pool_bytes))
-      return fail(SF_ERR_INVALID, "job sequence outside the pool");
-    if ((p.t_off & kStoreFlag) && !ctx->store)
-      return fail(SF_ERR_INVALID, "store text but the context uses no store");
-    keys.push_back({p.p_off, p.m, (uint32_t)(2 * q)});
-    keys.push_back({p.t_off, p.n, (uint32_t)(2 * q + 1)});
-  }
-  // In offset order: a pool built in job order (the usual case) needs no sort.
-  auto key_less = [](const Key& a, const Key& b) {
-    return a.off != b.off ? a.off < b.off : a.len < b.len;
+  // Sequence u is pass u / 2's pattern (u even) or text (u odd).  Pass order is already in
+  // (offset, length) order for a pool built in job order, the usual case: then no sort.
+  auto seq_of = [&](size_t u, uint64_t& off, uint32_t& len) {
+    const Pass& p = P->passes[u >> 1];
+    off = (u & 1) ? p.t_off : p.p_off;
+    len = (u & 1) ? p.n : p.m;
   };
-  if (!std::is_sorted(keys.begin(), keys.end(), key_less)) std::sort(keys.begin(), keys.end(), key_less);
-  std::vector<uint64_t> word_of(2 * np);
+  bool in_order = true;
+  {
+    uint64_t po = 0;
+    uint32_t pl = 0;
+    for (size_t q = 0; q < np; ++q) {
+      const Pass& p = P->passes[q];
+      if ((p.p_off & kOffMask) + p.m > P->pool_bytes ||
+          (!(p.t_off & kStoreFlag) && (p.t_off & kOffMask) + p.n > P->pool_bytes))
+        return fail(SF_ERR_INVALID, "job sequence outside the pool");
+      if ((p.t_off & kStoreFlag) && !ctx->store)
+        return fail(SF_ERR_INVALID, "store text but the context uses no store");
+      for (size_t h = 0; h < 2 && in_order; ++h) {
+        uint64_t o;
+        uint32_t l;
+        seq_of(2 * q + h, o, l);
+        if (q + h > 0 && (o < po || (o == po && l < pl))) in_order = false;
+        po = o;
+        pl = l;
+      }
+    }
+  }
+  std::vector<Key> keys;
+  if (!in_order) {
+    keys.reserve(2 * np);
+    for (size_t u = 0; u < 2 * np; ++u) {
+      Key k;
+      seq_of(u, k.off, k.len);
+      k.idx = (uint32_t)u;
+      keys.push_back(k);
+    }
+    std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+      return a.off != b.off ? a.off < b.off : a.len < b.len;
+    });
+  }
+  auto& word_of = S.word_of;
+  word_of.resize(2 * np);
   P->seq_boff.clear();
   P->seq_len.clear();
   P->seq_woff.clear();
-  uint64_t words = 0;
-  for (size_t q = 0; q < keys.size(); ++q) {
-    if (q == 0 || keys[q].off != keys[q - 1].off || keys[q].len != keys[q - 1].len) {
-      P->seq_boff.push_back(keys[q].off);
-      P->seq_len.push_back(keys[q].len);
-      P->seq_woff.push_back(words);
-      words += seq_words(keys[q].len);
+  P->seq_boff.reserve(2 * np);
+  P->seq_len.reserve(2 * np);
+  P->seq_woff.reserve(2 * np);
+  uint64_t words = 0, last_off = 0;
+  uint32_t last_len = 0;
+  for (size_t q = 0; q < 2 * np; ++q) {
+    uint64_t off;
+    uint32_t len, idx;
+    if (in_order) {
+      seq_of(q, off, len);
+      idx = (uint32_t)q;
+    } else {
+      off = keys[q].off;
+      len = keys[q].len;
+      idx = keys[q].idx;
     }
-    word_of[keys[q].idx] = P->seq_woff.back();
+    if (q == 0 || off != last_off || len != last_len) {
+      P->seq_boff.push_back(off);
+      P->seq_len.push_back(len);
+      P->seq_woff.push_back(words);
+      words += seq_words(len);
+      last_off = off;
+      last_len = len;
+    }
+    word_of[idx] = P->seq_woff.back();
   }
   P->pool_words = words + 256;  // slack: kernels read whole windows past a sequence's end
 
   // Per-kind arrays.
-  std::vector<DJob> dj;
-  std::vector<DParams> dp;
-  std::vector<TJob> tj;
-  std::vector<uint16_t> cls;
-  std::vector<MJob> mj;
-  dj.reserve(np);
-  dp.reserve(np);
-  tj.reserve(np);
-  cls.reserve(np);
-  std::vector<uint32_t> wlist;
+  auto& dj = S.dj;
+  auto& dp = S.dp;
+  auto& tj = S.tj;
+  auto& cls = S.cls;
+  auto& mj = S.mj;
+  auto& wlist = S.wlist;
+  wlist.clear();
   P->slot.assign(np, 0);
-  struct Item {
-    uint32_t slot;
-    uint64_t work;
-    uint64_t lat = 0;  // its warp's time, roughly: rows (steps) x the class's work per row
-  };
-  struct Key2 {
-    int kind, c, wide, tb, lanes;
-    bool operator<(const Key2& o) const {
-      return std::tie(kind, c, wide, tb, lanes) < std::tie(o.kind, o.c, o.wide, o.tb, o.lanes);
-    }
-    bool operator==(const Key2& o) const {
-      return kind == o.kind && c == o.c && wide == o.wide && tb == o.tb && lanes == o.lanes;
-    }
-  };
-  std::vector<std::pair<Key2, Item>> items;
+  auto& items = S.items;
+  items.clear();
   items.reserve(np);
   const bool use16 = allow16();
   const int lanes16 = default_lanes16();
@@ -328,98 +420,144 @@ int plan_build(sf_plan* P) {
       q += cnt;
     }
   }
-  // The tune table's answers, memoised per class (a batch has few classes).
-  struct TuneMemo {
-    ClassKey key;
-    int c, lanes;
-  };
-  std::vector<TuneMemo> memo;
-  auto tuned = [&](int kind, int& c, bool wide, bool tb, int& lanes) {
-    if (!tune || tune->empty()) return;
-    const ClassKey k{kind, c, wide ? 1 : 0, tb ? 1 : 0, lanes};
-    for (size_t u = memo.size(); u-- > 0;)
-      if (memo[u].key == k) {
-        c = memo[u].c;
-        lanes = memo[u].lanes;
-        return;
-      }
-    apply_tune(tune, kind, c, wide, tb, lanes);
-    memo.push_back(TuneMemo{k, c, lanes});
-  };
-  std::vector<uint64_t> pass_work(np, 0), pass_lat(np, 0);
-  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
+  // Slots in each kind's arrays, in pass order.  Myers classes are checked here, so that the
+  // parallel part below cannot fail.
+  size_t n_myers = 0;
   for (size_t q = 0; q < np; ++q) {
     const Pass& p = P->passes[q];
     if (p.kind == PK_MYERS) {
-      int b = 1, lanes = 1;
-      int rc = choose_myers_class(p.m, b, lanes);
+      int b = 1, l = 1;
+      const int rc = choose_myers_class(p.m, b, l);
       if (rc) return rc;
-      tuned(PK_MYERS, b, false, false, lanes);
-      MJob m{};
-      m.p_word = word_of[2 * q];
-      m.t_word = word_of[2 * q + 1];
-      m.m = p.m;
-      m.n = p.n;
-      m.mode = p.mode;
-      m.k = p.k;
-      P->slot[q] = (uint32_t)mj.size();
-      items.push_back({Key2{PK_MYERS, b, 0, 0, lanes},
-                       Item{(uint32_t)mj.size(), (uint64_t)p.n,
-                            ((uint64_t)p.n + (uint64_t)lanes) * (4u * (uint64_t)b + 4u)}});
-      mj.push_back(m);
-      continue;
+      P->slot[q] = (uint32_t)n_myers++;
+    } else {
+      P->slot[q] = (uint32_t)(q - n_myers);
     }
-    uint32_t flags = 0;
-    DJob j = make_djob(p, flags);
-    j.p_word = word_of[2 * q];
-    j.t_word = word_of[2 * q + 1];
-    j.p_byte = p.p_off & kOffMask;
-    const int64_t wmax = band_wmax(j, flags);
-    int c = 4;
-    bool wide = false;
-    PassKind kind = PK_AFFINE;
-    int ln = 32;
-    classify_affine(p, flags, wmax, use16, kind, c, wide, ln, lanes16);
-    const bool tb = p.want_cigar && p.kind != PK_LOCAL;
-    if (!wide) tuned(kind, c, false, tb, ln);
-    if (tb) {
-      flags |= F_TB;
-      j.tb_word = tb_words;
-      const int64_t chunks = wide ? wide_chunks(c, wmax) : 1;
-      tb_words += (uint64_t)p.m * (tb_row_words(c, chunks) * (uint64_t)ln / 32);
-    }
-    if (wide) scratch_cells = std::max<uint64_t>(scratch_cells, (uint64_t)wide_chunks(c, wmax) * 32 * c);
-    DParams pr{};
-    pr.flags = flags;
-    pr.xdrop = p.xdrop;
-    pr.bonus0 = p.bonus0;
-    pr.bonus1 = p.bonus1;
-    pr.mat = p.sc.mat;
-    pr.mis = p.sc.mis;
-    pr.open = p.sc.open;
-    pr.ext = p.sc.ext;
-    TJob t{};
-    if (tb) {
-      t.ops_off = ops_words;
-      const uint64_t cap = (uint64_t)p.m + p.n + 2;
-      t.ops_cap = (uint32_t)std::min<uint64_t>(cap, 0xffffffffull);
-      ops_words += cap;
-      t.kind = p.tb_kind;
-      t.end_bonus = p.end_bonus;
-      wlist.push_back((uint32_t)dj.size());
-    }
-    P->slot[q] = (uint32_t)dj.size();
-    const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
-    pass_work[q] = work;
-    const uint64_t row_cost = (uint64_t)c * (wide ? (uint64_t)wide_chunks(c, wmax) : 1u) + 8u;
-    pass_lat[q] = (uint64_t)std::max<uint32_t>(p.m, 1) * row_cost;
-    if (!P->chained[q])
-      items.push_back({Key2{kind, c, wide, tb, ln}, Item{(uint32_t)dj.size(), work, pass_lat[q]}});
-    dj.push_back(j);
-    dp.push_back(pr);
-    tj.push_back(t);
-    cls.push_back((uint16_t)(c | (wide ? 0x100 : 0) | (kind == PK_AFFINE16 ? 0x200 : 0)));
   }
+  const size_t n_affine = np - n_myers;
+  mj.resize(n_myers);
+  dj.resize(n_affine);
+  dp.resize(n_affine);
+  tj.resize(n_affine);
+  cls.resize(n_affine);
+  auto& pass_work = S.pass_work;
+  auto& pass_lat = S.pass_lat;
+  auto& tb_need = S.tb_need;
+  auto& ops_need = S.ops_need;
+  auto& per = S.per;
+  auto& has_item = S.has_item;
+  pass_work.assign(np, 0);
+  pass_lat.assign(np, 0);
+  tb_need.assign(n_affine, 0);
+  ops_need.assign(n_affine, 0);
+  per.resize(np);
+  has_item.assign(np, 0);
+  constexpr int kMaxThreads = 8;
+  uint64_t scratch_max[kMaxThreads] = {};
+  // Descriptors of passes [q0, q1), each written at its slot.
+  auto describe = [&](size_t q0, size_t q1, int worker) {
+    // The tune table's answers, memoised per class (a batch has few classes).
+    struct TuneMemo {
+      ClassKey key;
+      int c, lanes;
+    };
+    std::vector<TuneMemo> memo;
+    auto tuned = [&](int kind, int& c, bool wide, bool tb, int& lanes) {
+      if (!tune || tune->empty()) return;
+      const ClassKey k{kind, c, wide ? 1 : 0, tb ? 1 : 0, lanes};
+      for (size_t u = memo.size(); u-- > 0;)
+        if (memo[u].key == k) {
+          c = memo[u].c;
+          lanes = memo[u].lanes;
+          return;
+        }
+      apply_tune(tune, kind, c, wide, tb, lanes);
+      memo.push_back(TuneMemo{k, c, lanes});
+    };
+    for (size_t q = q0; q < q1; ++q) {
+      const Pass& p = P->passes[q];
+      const uint32_t sl = P->slot[q];
+      if (p.kind == PK_MYERS) {
+        int b = 1, lanes = 1;
+        (void)choose_myers_class(p.m, b, lanes);
+        tuned(PK_MYERS, b, false, false, lanes);
+        MJob& m = mj[sl];
+        m = MJob{};
+        m.p_word = word_of[2 * q];
+        m.t_word = word_of[2 * q + 1];
+        m.m = p.m;
+        m.n = p.n;
+        m.mode = p.mode;
+        m.k = p.k;
+        per[q] = {Key2{PK_MYERS, b, 0, 0, lanes},
+                  Item{sl, (uint64_t)p.n, ((uint64_t)p.n + (uint64_t)lanes) * (4u * (uint64_t)b + 4u)}};
+        has_item[q] = 1;
+        continue;
+      }
+      uint32_t flags = 0;
+      DJob j = make_djob(p, flags);
+      j.p_word = word_of[2 * q];
+      j.t_word = word_of[2 * q + 1];
+      j.p_byte = p.p_off & kOffMask;
+      const int64_t wmax = band_wmax(j, flags);
+      int c = 4;
+      bool wide = false;
+      PassKind kind = PK_AFFINE;
+      int ln = 32;
+      classify_affine(p, flags, wmax, use16, kind, c, wide, ln, lanes16);
+      const bool tb = p.want_cigar && p.kind != PK_LOCAL;
+      if (!wide) tuned(kind, c, false, tb, ln);
+      TJob t{};
+      if (tb) {
+        flags |= F_TB;
+        const int64_t chunks = wide ? wide_chunks(c, wmax) : 1;
+        tb_need[sl] = (uint64_t)p.m * (tb_row_words(c, chunks) * (uint64_t)ln / 32);
+        const uint64_t cap = (uint64_t)p.m + p.n + 2;
+        ops_need[sl] = cap;
+        t.ops_cap = (uint32_t)std::min<uint64_t>(cap, 0xffffffffull);
+        t.kind = p.tb_kind;
+        t.end_bonus = p.end_bonus;
+      }
+      if (wide)
+        scratch_max[worker] =
+            std::max<uint64_t>(scratch_max[worker], (uint64_t)wide_chunks(c, wmax) * 32 * c);
+      DParams pr{};
+      pr.flags = flags;
+      pr.xdrop = p.xdrop;
+      pr.bonus0 = p.bonus0;
+      pr.bonus1 = p.bonus1;
+      pr.mat = p.sc.mat;
+      pr.mis = p.sc.mis;
+      pr.open = p.sc.open;
+      pr.ext = p.sc.ext;
+      const uint64_t work = (uint64_t)std::max<uint32_t>(p.m, 1) * (uint64_t)std::max<int64_t>(wmax, 1);
+      pass_work[q] = work;
+      const uint64_t row_cost = (uint64_t)c * (wide ? (uint64_t)wide_chunks(c, wmax) : 1u) + 8u;
+      pass_lat[q] = (uint64_t)std::max<uint32_t>(p.m, 1) * row_cost;
+      if (!P->chained[q]) {
+        per[q] = {Key2{kind, c, wide, tb, ln}, Item{sl, work, pass_lat[q]}};
+        has_item[q] = 1;
+      }
+      dj[sl] = j;
+      dp[sl] = pr;
+      tj[sl] = t;
+      cls[sl] = (uint16_t)(c | (wide ? 0x100 : 0) | (kind == PK_AFFINE16 ? 0x200 : 0));
+    }
+  };
+  parallel_chunks(np, 4096, kMaxThreads, describe);
+  // Offsets in pass order: traceback words, CIGAR slots, the walk list; then the items.
+  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
+  for (int w = 0; w < kMaxThreads; ++w) scratch_cells = std::max(scratch_cells, scratch_max[w]);
+  for (size_t sl = 0; sl < n_affine; ++sl) {
+    if (!(dp[sl].flags & F_TB)) continue;
+    dj[sl].tb_word = tb_words;
+    tb_words += tb_need[sl];
+    tj[sl].ops_off = ops_words;
+    ops_words += ops_need[sl];
+    wlist.push_back((uint32_t)sl);
+  }
+  for (size_t q = 0; q < np; ++q)
+    if (has_item[q]) items.push_back(per[q]);
   // Chains: one work item each (longest first, as passes); per chained job its link; per
   // chain its snapshot rows, the sorted distinct resume rows (align.rs:2244-2246), and a
   // slot for each.
@@ -471,22 +609,37 @@ int plan_build(sf_plan* P) {
   // Buckets in key order; within a bucket, longest work first (ties in job order).  The
   // keys are few: a counting sort by bucket, then a sort by work inside each.
   std::vector<Key2> keys2;
-  std::vector<uint32_t> kid(items.size());
+  auto& kid = S.kid;
+  kid.resize(items.size());
   {
-    int last = -1;
+    // A key packs into 18 bits (kind < 8, C < 128, lanes <= 32): a direct table of key
+    // indices, reset after use.
+    static thread_local std::vector<int32_t> index_of(1u << 18, -1);
+    auto code = [](const Key2& k) {
+      return ((uint32_t)k.kind & 7u) << 15 | ((uint32_t)k.c & 127u) << 8 |
+             ((uint32_t)k.wide & 1u) << 7 | ((uint32_t)k.tb & 1u) << 6 |
+             ((uint32_t)k.lanes & 63u);
+    };
     for (size_t q = 0; q < items.size(); ++q) {
       const Key2& k = items[q].first;
-      if (last < 0 || !(keys2[last] == k)) {
-        last = -1;
+      int32_t& at = index_of[code(k)];
+      if (at < 0 || !(keys2[(size_t)at] == k)) {
+        // A code is unique per key within the bounds above; a key outside them (never
+        // built) falls back to a search.
+        int32_t f = -1;
         for (size_t u = 0; u < keys2.size(); ++u)
-          if (keys2[u] == k) last = (int)u;
-        if (last < 0) {
+          if (keys2[u] == k) f = (int32_t)u;
+        if (f < 0) {
           keys2.push_back(k);
-          last = (int)keys2.size() - 1;
+          f = (int32_t)keys2.size() - 1;
         }
+        if (at < 0) at = f;
+        kid[q] = (uint32_t)f;
+        continue;
       }
-      kid[q] = (uint32_t)last;
+      kid[q] = (uint32_t)at;
     }
+    for (const Key2& k : keys2) index_of[code(k)] = -1;
   }
   std::vector<uint32_t> rank(keys2.size());
   {
@@ -501,12 +654,14 @@ int plan_build(sf_plan* P) {
     bwork[kid[q]] += items[q].second.work;
   }
   for (size_t u = 0; u < keys2.size(); ++u) start[u + 1] += start[u];
-  std::vector<std::pair<uint64_t, uint32_t>> byb(items.size());  // (work, job order) by bucket
+  auto& byb = S.byb;  // (work, job order) by bucket
+  byb.resize(items.size());
   {
     std::vector<uint64_t> at(start.begin(), start.end() - 1);
     for (size_t q = 0; q < items.size(); ++q) byb[at[rank[kid[q]]]++] = {items[q].second.work, (uint32_t)q};
   }
-  std::vector<uint32_t> order(items.size());
+  auto& order = S.order;
+  order.resize(items.size());
   P->buckets.clear();
   std::vector<Key2> sorted_keys(keys2.size());
   for (size_t u = 0; u < keys2.size(); ++u) sorted_keys[rank[u]] = keys2[u];
@@ -522,7 +677,7 @@ int plan_build(sf_plan* P) {
   };
   constexpr uint32_t kBins = 16 * 61 + 16;
   std::vector<uint32_t> bin_at(kBins + 1);
-  std::vector<std::pair<uint64_t, uint32_t>> tmp;
+  auto& tmp = S.tmp;
   for (size_t u = 0; u < sorted_keys.size(); ++u) {
     auto b0 = byb.begin() + (ptrdiff_t)start[u], b1 = byb.begin() + (ptrdiff_t)start[u + 1];
     {
@@ -623,7 +778,8 @@ int plan_build(sf_plan* P) {
   };
   {
     // Sequence table: byte offsets, word offsets (both 8-byte aligned), then lengths.
-    std::vector<uint8_t> st(seq_bytes);
+    auto& st = S.seq_table;
+    st.resize(seq_bytes);
     std::memcpy(st.data(), P->seq_boff.data(), nseq * 8);
     std::memcpy(st.data() + nseq * 8, P->seq_woff.data(), nseq * 8);
     std::memcpy(st.data() + nseq * 16, P->seq_len.data(), nseq * 4);
@@ -1048,75 +1204,96 @@ void count_sorted(const std::vector<Pass>& ps, size_t q0, size_t count, R res) {
   }
 }
 
+// One job's pass, or the job's error (recorded for the calling thread).
+int job_to_pass(const sf_job_t& j, const sf_affine_t* scores, uint32_t n_scores,
+                uint64_t pool_bytes, const sf_store* store, Pass& p) {
+  p = Pass{};
+  p.p_off = j.p_off;
+  p.t_off = j.t_off;
+  p.m = j.m;
+  p.n = j.n;
+  if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
+  if (j.text_src > SF_TEXT_STORE_REV) return fail(SF_ERR_INVALID, "bad text source");
+  if (j.p_off > pool_bytes || j.m > pool_bytes - j.p_off)
+    return fail(SF_ERR_INVALID, "job sequence outside the pool");
+  if (j.text_src == SF_TEXT_STORE || j.text_src == SF_TEXT_STORE_REV) {
+    if (!store) return fail(SF_ERR_INVALID, "store text but the context uses no store");
+    if (j.t_off > store->bases || j.n > store->bases - j.t_off)
+      return fail(SF_ERR_INVALID, "text window outside the store");
+    p.t_off = kStoreFlag | (j.text_src == SF_TEXT_STORE_REV ? kRevFlag : 0) |
+              (j.t_off + kStorePad);
+  } else if (j.t_off > pool_bytes || j.n > pool_bytes - j.t_off) {
+    return fail(SF_ERR_INVALID, "job sequence outside the pool");
+  }
+  if (j.kind != SF_JOB_MYERS) {
+    if (j.sc_index >= n_scores || !ok_sc(&scores[j.sc_index]))
+      return fail(SF_ERR_INVALID, "bad scoring index");
+    p.sc = scores[j.sc_index];
+  }
+  switch (j.kind) {
+    case SF_JOB_MYERS:
+      if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
+      p.kind = PK_MYERS;
+      p.mode = j.mode;
+      p.k = j.k;
+      break;
+    case SF_JOB_AFFINE:
+      if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
+      p.kind = PK_AFFINE;
+      p.mode = j.mode;
+      p.band = j.band;
+      p.geom = j.n;
+      p.want_cigar = j.want_cigar != 0;
+      p.tb_kind = 0;
+      break;
+    case SF_JOB_EXTEND_WINDOW:
+      p.kind = PK_AFFINE;
+      p.mode = SF_PREFIX;
+      p.band = j.band;
+      p.geom = std::max<uint64_t>(j.window, j.n);
+      p.clip = true;
+      p.cell = true;
+      p.xdrop = j.xdrop;
+      p.end_bonus = j.end_bonus;
+      p.want_cigar = j.want_cigar != 0;
+      p.tb_kind = 1;
+      break;
+    case SF_JOB_LOCAL:
+      p.kind = PK_LOCAL;
+      p.dlo = j.dlo;
+      p.dhi = j.dhi;
+      p.bonus0 = j.end_bonus;
+      p.bonus1 = j.end_bonus2;
+      break;
+    default:
+      return fail(SF_ERR_INVALID, "bad job kind");
+  }
+  return SF_OK;
+}
+
 int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
                           uint32_t n_scores, uint64_t pool_bytes, std::vector<Pass>& ps,
                           const sf_store* store) {
-  ps.clear();
-  ps.reserve(count);
-  for (uint64_t q = 0; q < count; ++q) {
-    const sf_job_t& j = jobs[q];
+  ps.resize(count);
+  // Chunks in parallel; each stops at its first bad job, and the first bad job of all is
+  // converted again here, so that its error is the calling thread's.
+  constexpr int kMaxThreads = 8;
+  uint64_t first_bad[kMaxThreads];
+  for (int w = 0; w < kMaxThreads; ++w) first_bad[w] = UINT64_MAX;
+  parallel_chunks(count, 8192, kMaxThreads, [&](size_t q0, size_t q1, int w) {
+    for (size_t q = q0; q < q1; ++q)
+      if (job_to_pass(jobs[q], scores, n_scores, pool_bytes, store, ps[q]) != SF_OK) {
+        first_bad[w] = std::min<uint64_t>(first_bad[w], q);
+        return;
+      }
+  });
+  uint64_t bad = UINT64_MAX;
+  for (int w = 0; w < kMaxThreads; ++w) bad = std::min(bad, first_bad[w]);
+  if (bad != UINT64_MAX) {
     Pass p;
-    p.p_off = j.p_off;
-    p.t_off = j.t_off;
-    p.m = j.m;
-    p.n = j.n;
-    if (j.m >= 0x7fffffffu || j.n >= 0x7fffffffu) return fail(SF_ERR_TOO_LONG, "sequence too long");
-    if (j.text_src > SF_TEXT_STORE_REV) return fail(SF_ERR_INVALID, "bad text source");
-    if (j.p_off > pool_bytes || j.m > pool_bytes - j.p_off)
-      return fail(SF_ERR_INVALID, "job sequence outside the pool");
-    if (j.text_src == SF_TEXT_STORE || j.text_src == SF_TEXT_STORE_REV) {
-      if (!store) return fail(SF_ERR_INVALID, "store text but the context uses no store");
-      if (j.t_off > store->bases || j.n > store->bases - j.t_off)
-        return fail(SF_ERR_INVALID, "text window outside the store");
-      p.t_off = kStoreFlag | (j.text_src == SF_TEXT_STORE_REV ? kRevFlag : 0) |
-                (j.t_off + kStorePad);
-    } else if (j.t_off > pool_bytes || j.n > pool_bytes - j.t_off) {
-      return fail(SF_ERR_INVALID, "job sequence outside the pool");
-    }
-    if (j.kind != SF_JOB_MYERS) {
-      if (j.sc_index >= n_scores || !ok_sc(&scores[j.sc_index]))
-        return fail(SF_ERR_INVALID, "bad scoring index");
-      p.sc = scores[j.sc_index];
-    }
-    switch (j.kind) {
-      case SF_JOB_MYERS:
-        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
-        p.kind = PK_MYERS;
-        p.mode = j.mode;
-        p.k = j.k;
-        break;
-      case SF_JOB_AFFINE:
-        if (!ok_mode(j.mode)) return fail(SF_ERR_INVALID, "bad mode");
-        p.kind = PK_AFFINE;
-        p.mode = j.mode;
-        p.band = j.band;
-        p.geom = j.n;
-        p.want_cigar = j.want_cigar != 0;
-        p.tb_kind = 0;
-        break;
-      case SF_JOB_EXTEND_WINDOW:
-        p.kind = PK_AFFINE;
-        p.mode = SF_PREFIX;
-        p.band = j.band;
-        p.geom = std::max<uint64_t>(j.window, j.n);
-        p.clip = true;
-        p.cell = true;
-        p.xdrop = j.xdrop;
-        p.end_bonus = j.end_bonus;
-        p.want_cigar = j.want_cigar != 0;
-        p.tb_kind = 1;
-        break;
-      case SF_JOB_LOCAL:
-        p.kind = PK_LOCAL;
-        p.dlo = j.dlo;
-        p.dhi = j.dhi;
-        p.bonus0 = j.end_bonus;
-        p.bonus1 = j.end_bonus2;
-        break;
-      default:
-        return fail(SF_ERR_INVALID, "bad job kind");
-    }
-    ps.push_back(p);
+    const int rc = job_to_pass(jobs[bad], scores, n_scores, pool_bytes, store, p);
+    ps.clear();
+    return rc;
   }
   return SF_OK;
 }
