@@ -604,6 +604,7 @@ def main():
     d2h = int(res.nbytes + used.value * 4)
     e2e = {"value": e2e_cells * ws / e2e_s / 1e9, "unit": "GCUPS", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+           "pairs_per_s": len(pairs_list[-1]) * ws / e2e_s,
            "call": "sf_batch_run (C ABI), pinned host pool"}
 
     # Plain form: one launch (one C-ABI call) per pair on a sample.
@@ -666,6 +667,7 @@ def main():
                                            for g in tune_report["groups"]
                                            if (g["chosen"]["c"], g["chosen"]["lanes"]) !=
                                            (g["c"], g["lanes"])]}},
+                "pairs_per_s": len(pairs_list[-1]) * ws / (ms * 1e-3),
                 "e2e": e2e, "plain": plain,
                 "batched_vs_plain": (value / plain["value"]) if plain else None,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
