@@ -297,7 +297,10 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
     if (D1 && i > 1) {
       const uint32_t s0 = sel[0];
       uint32_t nx = __shfl_down_sync(FULL, s0, 1);
-      const uint32_t far = sel_byte(base_at(a.pool, x.J.t_word, (uint64_t)(lo + 32 * C - 1)));
+      // The column entering lane 31 (32-bit positions: texts are shorter than 2^31).
+      const uint32_t fcol = (uint32_t)(lo + 32 * C - 1);
+      const uint32_t fw = __ldg(a.pool + x.J.t_word + (fcol >> 4));
+      const uint32_t far = sel_byte((fw >> (2u * (fcol & 15u))) & 3u);
       if (lane == 31) nx = far;
 #pragma unroll
       for (int k = 0; k + 1 < C2; ++k) sel[k] = sel[k + 1];

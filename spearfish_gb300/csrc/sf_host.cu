@@ -349,7 +349,7 @@ int plan_build(sf_plan* P) {
     }
     word_of[idx] = P->seq_woff.back();
   }
-  P->pool_words = words + 256;  // slack: kernels read whole windows past a sequence's end
+  P->pool_words = words + 512;  // slack: kernels read whole windows past a sequence's end
 
   // Per-kind arrays.
   auto& dj = S.dj;
