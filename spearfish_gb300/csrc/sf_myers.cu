@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
       uint32_t pos = l == 0 ? (uint32_t)top : (in >> 1) & 1u;
       uint32_t neg = l == 0 ? 0u : in & 1u;
       // eq(c) from the bit planes: both code bits equal c's.
-      const uint64_t m0 = (c & 1u) ? ~0ull : 0ull, m1 = (c & 2u) ? ~0ull : 0ull;
+      [[maybe_unused]] const uint64_t m0 = (c & 1u) ? ~0ull : 0ull, m1 = (c & 2u) ? ~0ull : 0ull;
       int hlast = 0;
 #pragma unroll
       for (int bb = 0; bb < B; ++bb) {
