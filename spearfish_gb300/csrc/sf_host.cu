@@ -7,6 +7,9 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <deque>
+#include <condition_variable>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -15,6 +18,8 @@
 #include <tuple>
 #include <unordered_map>
 #include <vector>
+
+#include <unistd.h>
 
 #include "sf_engine.h"
 
@@ -236,29 +241,101 @@ namespace sfe {
 
 uint64_t seq_words(uint64_t len) { return (len + 1 + 15) / 16; }
 
-// f(begin, end, worker) over [0, n) in contiguous chunks: on up to max_threads host threads
-// when every thread gets at least min_per_thread items, else (or when threads cannot be
-// started) on the calling thread alone.
+// Host worker threads for the plan build, started on first use and kept for the process:
+// starting threads per call would cost more than small batches save.  A process that forks
+// gets a fresh pool in the child (the parent's threads do not exist there).
+class HostPool {
+ public:
+  static HostPool& get() {
+    static std::mutex mu;
+    static HostPool* pool = nullptr;
+    std::lock_guard<std::mutex> g(mu);
+    if (!pool || pool->pid_ != getpid()) pool = new HostPool();  // a child's old pool is abandoned
+    return *pool;
+  }
+  size_t workers() const { return threads_.size(); }
+  // Queues fn; returns false if it could not be queued.
+  bool post(std::function<void()> fn) {
+    try {
+      std::lock_guard<std::mutex> g(m_);
+      q_.push_back(std::move(fn));
+    } catch (...) {
+      return false;
+    }
+    cv_.notify_one();
+    return true;
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned n = std::min(7u, hw > 1 ? hw - 1 : 0u);
+    try {
+      for (unsigned k = 0; k < n; ++k) threads_.emplace_back([this] { loop(); });
+    } catch (...) {
+    }
+    for (auto& t : threads_) t.detach();
+  }
+  void loop() {
+    for (;;) {
+      std::function<void()> fn;
+      {
+        std::unique_lock<std::mutex> g(m_);
+        cv_.wait(g, [this] { return !q_.empty(); });
+        fn = std::move(q_.front());
+        q_.pop_front();
+      }
+      fn();
+    }
+  }
+  pid_t pid_;
+  std::vector<std::thread> threads_;
+  std::mutex m_;
+  std::condition_variable cv_;
+  std::deque<std::function<void()>> q_;
+};
+
+// f(begin, end, k) for the k-th of up to max_threads contiguous chunks of [0, n), chunks 1..
+// on the host pool's threads, when every chunk gets at least min_per_thread items (else one
+// chunk on the calling thread).  The same (n, min_per_thread, max_threads) always gives the
+// same chunks; a chunk the pool cannot take runs on the calling thread.
 template <class F>
 void parallel_chunks(size_t n, size_t min_per_thread, int max_threads, F&& f) {
-  const unsigned hw = std::thread::hardware_concurrency();
-  size_t t = std::min<size_t>({(size_t)(hw ? hw : 1), (size_t)max_threads,
+  HostPool& pool = HostPool::get();
+  size_t t = std::min<size_t>({pool.workers() + 1, (size_t)max_threads,
                                min_per_thread ? n / min_per_thread : 1});
   if (t <= 1) {
     f(size_t(0), n, 0);
     return;
   }
   const size_t chunk = (n + t - 1) / t;
-  std::vector<std::thread> th;
-  try {
-    for (size_t k = 1; k < t; ++k)
-      th.emplace_back([&f, k, chunk, n] { f(k * chunk, std::min(n, (k + 1) * chunk), (int)k); });
-  } catch (...) {
-    // Run the chunks no thread took here.
-    for (size_t k = th.size() + 1; k < t; ++k) f(k * chunk, std::min(n, (k + 1) * chunk), 0);
+  struct Done {
+    std::mutex m;
+    std::condition_variable cv;
+    size_t left = 0;
+  } done;
+  for (size_t k = 1; k < t; ++k) {
+    const size_t b = k * chunk, e = std::min(n, (k + 1) * chunk);
+    {
+      std::lock_guard<std::mutex> g(done.m);
+      ++done.left;
+    }
+    const bool queued = pool.post([&f, &done, b, e, k] {
+      f(b, e, (int)k);
+      std::lock_guard<std::mutex> g(done.m);
+      if (--done.left == 0) done.cv.notify_all();
+    });
+    if (!queued) {
+      {
+        std::lock_guard<std::mutex> g(done.m);
+        --done.left;
+      }
+      f(b, e, (int)k);
+    }
   }
   f(size_t(0), std::min(n, chunk), 0);
-  for (auto& x : th) x.join();
+  std::unique_lock<std::mutex> g(done.m);
+  done.cv.wait(g, [&] { return done.left == 0; });
 }
 
 // Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
@@ -284,25 +361,50 @@ int plan_build(sf_plan* P) {
     off = (u & 1) ? p.t_off : p.p_off;
     len = (u & 1) ? p.n : p.m;
   };
+  constexpr int kChunks = 8;
   bool in_order = true;
   {
-    uint64_t po = 0;
-    uint32_t pl = 0;
-    for (size_t q = 0; q < np; ++q) {
-      const Pass& p = P->passes[q];
+    auto bad_pass = [&](const Pass& p) {
+      return (p.p_off & kOffMask) + p.m > P->pool_bytes ||
+             (!(p.t_off & kStoreFlag) && (p.t_off & kOffMask) + p.n > P->pool_bytes) ||
+             ((p.t_off & kStoreFlag) && !ctx->store);
+    };
+    uint64_t first_bad[kChunks];
+    bool ordered[kChunks];
+    for (int k = 0; k < kChunks; ++k) {
+      first_bad[k] = UINT64_MAX;
+      ordered[k] = true;
+    }
+    parallel_chunks(np, 8192, kChunks, [&](size_t q0, size_t q1, int k) {
+      uint64_t po = 0;
+      uint32_t pl = 0;
+      if (q0 > 0) seq_of(2 * q0 - 1, po, pl);
+      for (size_t q = q0; q < q1; ++q) {
+        if (bad_pass(P->passes[q])) {
+          first_bad[k] = q;
+          return;
+        }
+        for (size_t h = 0; h < 2; ++h) {
+          uint64_t o;
+          uint32_t l;
+          seq_of(2 * q + h, o, l);
+          if (q + h > 0 && (o < po || (o == po && l < pl))) ordered[k] = false;
+          po = o;
+          pl = l;
+        }
+      }
+    });
+    uint64_t bad = UINT64_MAX;
+    for (int k = 0; k < kChunks; ++k) {
+      bad = std::min(bad, first_bad[k]);
+      in_order = in_order && ordered[k];
+    }
+    if (bad != UINT64_MAX) {
+      const Pass& p = P->passes[bad];
       if ((p.p_off & kOffMask) + p.m > P->pool_bytes ||
           (!(p.t_off & kStoreFlag) && (p.t_off & kOffMask) + p.n > P->pool_bytes))
         return fail(SF_ERR_INVALID, "job sequence outside the pool");
-      if ((p.t_off & kStoreFlag) && !ctx->store)
-        return fail(SF_ERR_INVALID, "store text but the context uses no store");
-      for (size_t h = 0; h < 2 && in_order; ++h) {
-        uint64_t o;
-        uint32_t l;
-        seq_of(2 * q + h, o, l);
-        if (q + h > 0 && (o < po || (o == po && l < pl))) in_order = false;
-        po = o;
-        pl = l;
-      }
+      return fail(SF_ERR_INVALID, "store text but the context uses no store");
     }
   }
   std::vector<Key> keys;
@@ -326,28 +428,80 @@ int plan_build(sf_plan* P) {
   P->seq_boff.reserve(2 * np);
   P->seq_len.reserve(2 * np);
   P->seq_woff.reserve(2 * np);
-  uint64_t words = 0, last_off = 0;
-  uint32_t last_len = 0;
-  for (size_t q = 0; q < 2 * np; ++q) {
-    uint64_t off;
-    uint32_t len, idx;
-    if (in_order) {
-      seq_of(q, off, len);
-      idx = (uint32_t)q;
-    } else {
-      off = keys[q].off;
-      len = keys[q].len;
-      idx = keys[q].idx;
+  uint64_t words = 0;
+  if (in_order) {
+    // Two passes over chunks: count each chunk's new sequences and words, then write them
+    // at their places (a sequence equal to the one before it shares its words).
+    const size_t ns = 2 * np;
+    size_t cnt[kChunks] = {}, at0[kChunks] = {};
+    uint64_t wsum[kChunks] = {}, w0[kChunks] = {};
+    parallel_chunks(ns, 16384, kChunks, [&](size_t u0, size_t u1, int k) {
+      uint64_t po = 0;
+      uint32_t pl = 0;
+      if (u0 > 0) seq_of(u0 - 1, po, pl);
+      for (size_t u = u0; u < u1; ++u) {
+        uint64_t o;
+        uint32_t l;
+        seq_of(u, o, l);
+        if (u == 0 || o != po || l != pl) {
+          cnt[k]++;
+          wsum[k] += seq_words(l);
+        }
+        po = o;
+        pl = l;
+      }
+    });
+    size_t total = 0;
+    for (int k = 0; k < kChunks; ++k) {
+      at0[k] = total;
+      w0[k] = words;
+      total += cnt[k];
+      words += wsum[k];
     }
-    if (q == 0 || off != last_off || len != last_len) {
-      P->seq_boff.push_back(off);
-      P->seq_len.push_back(len);
-      P->seq_woff.push_back(words);
-      words += seq_words(len);
-      last_off = off;
-      last_len = len;
+    P->seq_boff.resize(total);
+    P->seq_len.resize(total);
+    P->seq_woff.resize(total);
+    parallel_chunks(ns, 16384, kChunks, [&](size_t u0, size_t u1, int k) {
+      size_t at = at0[k];
+      uint64_t w = w0[k], cur = 0, po = 0;
+      uint32_t pl = 0;
+      if (u0 > 0) {
+        seq_of(u0 - 1, po, pl);
+        cur = w - seq_words(pl);  // the last sequence before the chunk ends where it starts
+      }
+      for (size_t u = u0; u < u1; ++u) {
+        uint64_t o;
+        uint32_t l;
+        seq_of(u, o, l);
+        if (u == 0 || o != po || l != pl) {
+          P->seq_boff[at] = o;
+          P->seq_len[at] = l;
+          P->seq_woff[at] = w;
+          cur = w;
+          w += seq_words(l);
+          ++at;
+        }
+        word_of[u] = cur;
+        po = o;
+        pl = l;
+      }
+    });
+  } else {
+    uint64_t last_off = 0;
+    uint32_t last_len = 0;
+    for (size_t q = 0; q < 2 * np; ++q) {
+      const uint64_t off = keys[q].off;
+      const uint32_t len = keys[q].len;
+      if (q == 0 || off != last_off || len != last_len) {
+        P->seq_boff.push_back(off);
+        P->seq_len.push_back(len);
+        P->seq_woff.push_back(words);
+        words += seq_words(len);
+        last_off = off;
+        last_len = len;
+      }
+      word_of[keys[q].idx] = P->seq_woff.back();
     }
-    word_of[idx] = P->seq_woff.back();
   }
   P->pool_words = words + 512;  // slack: kernels read whole windows past a sequence's end
 
@@ -771,7 +925,14 @@ int plan_build(sf_plan* P) {
   size_t at = 0;
   auto put = [&](DevBuf& d, const void* src, size_t bytes) -> int {
     if (!bytes) return SF_OK;
-    std::memcpy(h + at, src, bytes);
+    // Large descriptor arrays are copied into the pinned staging on host threads.
+    constexpr size_t kPiece = size_t(1) << 20;
+    uint8_t* dst = h + at;
+    const uint8_t* from = static_cast<const uint8_t*>(src);
+    parallel_chunks((bytes + kPiece - 1) / kPiece, 2, 8, [&](size_t k0, size_t k1, int) {
+      const size_t b0 = k0 * kPiece, b1 = std::min(bytes, k1 * kPiece);
+      if (b1 > b0) std::memcpy(dst + b0, from + b0, b1 - b0);
+    });
     cudaError_t e = cudaMemcpyAsync(d.p, h + at, bytes, cudaMemcpyHostToDevice, ctx->s);
     at += (bytes + 15) & ~size_t(15);
     return e == cudaSuccess ? SF_OK : fail(SF_ERR_CUDA, cudaGetErrorString(e));
@@ -1309,49 +1470,56 @@ int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_c
   const DRes* rs = P->h_res.as<DRes>();
   const TRes* tr = P->h_tres.as<TRes>();
   const uint32_t* mo = P->h_mout.as<uint32_t>();
-  uint64_t acc = 0;
-  // Compacted op order = walk-list order = pass order among CIGAR passes.
-  for (size_t q = 0; q < P->passes.size(); ++q) {
-    const Pass& p = P->passes[q];
-    sf_result_t& o = results[q];
-    std::memset(&o, 0, sizeof o);
-    const uint32_t s = P->slot[q];
-    if (p.kind == PK_MYERS) {
-      o.distance = mo[s];
-      o.score = 0;
-      o.cells = (uint64_t)p.m * p.n;
-      continue;
-    }
-    const DRes& d = rs[s];
-    o.distance = SF_NONE;
-    o.cells = d.cells;
-    o.text_read = d.text_read;
-    if (p.kind == PK_LOCAL) {
-      o.score = d.score;
-    } else if (p.tb_kind == 1) {
-      const int32_t whole = sat_add32(d.score, p.end_bonus);
-      if (d.clip_best >= whole) {
-        o.score = d.clip_best;
-        o.pattern_end = d.clip_i;
-        o.text_end = d.clip_j;
+  const size_t np = P->passes.size();
+  parallel_chunks(np, 8192, 8, [&](size_t q0, size_t q1, int) {
+    for (size_t q = q0; q < q1; ++q) {
+      const Pass& p = P->passes[q];
+      sf_result_t& o = results[q];
+      std::memset(&o, 0, sizeof o);
+      const uint32_t s = P->slot[q];
+      if (p.kind == PK_MYERS) {
+        o.distance = mo[s];
+        o.score = 0;
+        o.cells = (uint64_t)p.m * p.n;
+        continue;
+      }
+      const DRes& d = rs[s];
+      o.distance = SF_NONE;
+      o.cells = d.cells;
+      o.text_read = d.text_read;
+      if (p.kind == PK_LOCAL) {
+        o.score = d.score;
+      } else if (p.tb_kind == 1) {
+        const int32_t whole = sat_add32(d.score, p.end_bonus);
+        if (d.clip_best >= whole) {
+          o.score = d.clip_best;
+          o.pattern_end = d.clip_i;
+          o.text_end = d.clip_j;
+        } else {
+          o.score = whole;
+          o.pattern_end = p.m;
+          o.text_end = d.score_col;
+        }
       } else {
-        o.score = whole;
+        o.score = d.score;
         o.pattern_end = p.m;
         o.text_end = d.score_col;
       }
-    } else {
-      o.score = d.score;
-      o.pattern_end = p.m;
-      o.text_end = d.score_col;
+      if (p.want_cigar && p.kind != PK_LOCAL) {
+        const TRes& t = tr[s];
+        o.status = t.status;
+        o.text_start = t.text_start;
+        o.n_ops = t.status == 0 ? t.n_ops : 0;
+      }
     }
-    if (p.want_cigar && p.kind != PK_LOCAL) {
-      const TRes& t = tr[s];
-      o.status = t.status;
-      o.text_start = t.text_start;
-      o.cigar_off = acc;
-      o.n_ops = t.status == 0 ? t.n_ops : 0;
-      acc += o.n_ops;
-    }
+  });
+  // Compacted op order = walk-list order = pass order among CIGAR passes.
+  uint64_t acc = 0;
+  for (size_t q = 0; q < np; ++q) {
+    const Pass& p = P->passes[q];
+    if (!p.want_cigar || p.kind == PK_LOCAL || p.kind == PK_MYERS) continue;
+    results[q].cigar_off = acc;
+    acc += results[q].n_ops;
   }
   return SF_OK;
 }
