@@ -225,7 +225,7 @@ struct BuildScratch {
   std::vector<uint32_t> wlist, kid, order;
   std::vector<std::pair<BucketKey, BucketItem>> items, per;
   std::vector<uint8_t> has_item, seq_table;
-  std::vector<std::pair<uint64_t, uint32_t>> byb, tmp;
+  std::vector<std::pair<uint64_t, uint32_t>> byb;
 };
 
 }  // namespace sfe
@@ -375,7 +375,7 @@ int plan_build(sf_plan* P) {
       first_bad[k] = UINT64_MAX;
       ordered[k] = true;
     }
-    parallel_chunks(np, 8192, kChunks, [&](size_t q0, size_t q1, int k) {
+    parallel_chunks(np, 2048, kChunks, [&](size_t q0, size_t q1, int k) {
       uint64_t po = 0;
       uint32_t pl = 0;
       if (q0 > 0) seq_of(2 * q0 - 1, po, pl);
@@ -435,7 +435,7 @@ int plan_build(sf_plan* P) {
     const size_t ns = 2 * np;
     size_t cnt[kChunks] = {}, at0[kChunks] = {};
     uint64_t wsum[kChunks] = {}, w0[kChunks] = {};
-    parallel_chunks(ns, 16384, kChunks, [&](size_t u0, size_t u1, int k) {
+    parallel_chunks(ns, 4096, kChunks, [&](size_t u0, size_t u1, int k) {
       uint64_t po = 0;
       uint32_t pl = 0;
       if (u0 > 0) seq_of(u0 - 1, po, pl);
@@ -461,7 +461,7 @@ int plan_build(sf_plan* P) {
     P->seq_boff.resize(total);
     P->seq_len.resize(total);
     P->seq_woff.resize(total);
-    parallel_chunks(ns, 16384, kChunks, [&](size_t u0, size_t u1, int k) {
+    parallel_chunks(ns, 4096, kChunks, [&](size_t u0, size_t u1, int k) {
       size_t at = at0[k];
       uint64_t w = w0[k], cur = 0, po = 0;
       uint32_t pl = 0;
@@ -698,7 +698,7 @@ int plan_build(sf_plan* P) {
       cls[sl] = (uint16_t)(c | (wide ? 0x100 : 0) | (kind == PK_AFFINE16 ? 0x200 : 0));
     }
   };
-  parallel_chunks(np, 4096, kMaxThreads, describe);
+  parallel_chunks(np, 2048, kMaxThreads, describe);
   // Offsets in pass order: traceback words, CIGAR slots, the walk list; then the items.
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   for (int w = 0; w < kMaxThreads; ++w) scratch_cells = std::max(scratch_cells, scratch_max[w]);
@@ -830,32 +830,34 @@ int plan_build(sf_plan* P) {
     return (uint32_t)(16 * (e - 3) + ((w >> (e - 4)) & 15));
   };
   constexpr uint32_t kBins = 16 * 61 + 16;
-  std::vector<uint32_t> bin_at(kBins + 1);
-  auto& tmp = S.tmp;
-  for (size_t u = 0; u < sorted_keys.size(); ++u) {
-    auto b0 = byb.begin() + (ptrdiff_t)start[u], b1 = byb.begin() + (ptrdiff_t)start[u + 1];
-    {
+  // Buckets sort their items independently: on the host pool for large batches.
+  P->buckets.assign(sorted_keys.size(), Bucket{});
+  parallel_chunks(sorted_keys.size(), items.size() >= 16384 ? 1 : sorted_keys.size() + 1, 8,
+                  [&](size_t u0, size_t u1, int) {
+    std::vector<uint32_t> bin_at(kBins + 1);
+    std::vector<std::pair<uint64_t, uint32_t>> tmp;
+    for (size_t u = u0; u < u1; ++u) {
+      auto b0 = byb.begin() + (ptrdiff_t)start[u], b1 = byb.begin() + (ptrdiff_t)start[u + 1];
       std::fill(bin_at.begin(), bin_at.end(), 0u);
       for (auto it = b0; it != b1; ++it) bin_at[kBins - 1 - wbin(it->first) + 1]++;
       for (uint32_t k = 0; k < kBins; ++k) bin_at[k + 1] += bin_at[k];
       tmp.assign(b0, b1);
       for (const auto& e : tmp) *(b0 + bin_at[kBins - 1 - wbin(e.first)]++) = e;
+      Bucket& b = P->buckets[u];
+      b.kind = (PassKind)sorted_keys[u].kind;
+      b.c = sorted_keys[u].c;
+      b.wide = sorted_keys[u].wide;
+      b.tb = sorted_keys[u].tb;
+      b.lanes = sorted_keys[u].lanes;
+      b.first = (uint32_t)start[u];
+      b.count = (uint32_t)(start[u + 1] - start[u]);
+      b.work = bwork[u];
+      for (auto it = b0; it != b1; ++it) {
+        order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
+        b.lat = std::max(b.lat, items[it->second].second.lat);
+      }
     }
-    Bucket b;
-    b.kind = (PassKind)sorted_keys[u].kind;
-    b.c = sorted_keys[u].c;
-    b.wide = sorted_keys[u].wide;
-    b.tb = sorted_keys[u].tb;
-    b.lanes = sorted_keys[u].lanes;
-    b.first = (uint32_t)start[u];
-    b.count = (uint32_t)(start[u + 1] - start[u]);
-    b.work = bwork[u];
-    for (auto it = b0; it != b1; ++it) {
-      order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
-      b.lat = std::max(b.lat, items[it->second].second.lat);
-    }
-    P->buckets.push_back(b);
-  }
+  });
   // Launch order: the buckets whose longest pass takes longest first, so that a few long
   // passes (a small grid) run beside the bulk instead of after it.
   std::stable_sort(P->buckets.begin(), P->buckets.end(),
@@ -1441,7 +1443,7 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
   constexpr int kMaxThreads = 8;
   uint64_t first_bad[kMaxThreads];
   for (int w = 0; w < kMaxThreads; ++w) first_bad[w] = UINT64_MAX;
-  parallel_chunks(count, 8192, kMaxThreads, [&](size_t q0, size_t q1, int w) {
+  parallel_chunks(count, 2048, kMaxThreads, [&](size_t q0, size_t q1, int w) {
     for (size_t q = q0; q < q1; ++q)
       if (job_to_pass(jobs[q], scores, n_scores, pool_bytes, store, ps[q]) != SF_OK) {
         first_bad[w] = std::min<uint64_t>(first_bad[w], q);
@@ -1471,7 +1473,7 @@ int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_c
   const TRes* tr = P->h_tres.as<TRes>();
   const uint32_t* mo = P->h_mout.as<uint32_t>();
   const size_t np = P->passes.size();
-  parallel_chunks(np, 8192, 8, [&](size_t q0, size_t q1, int) {
+  parallel_chunks(np, 2048, 8, [&](size_t q0, size_t q1, int) {
     for (size_t q = q0; q < q1; ++q) {
       const Pass& p = P->passes[q];
       sf_result_t& o = results[q];
