@@ -23,7 +23,16 @@
  *    current device, as the reference keeps per-thread DP buffers
  *    (align.rs:2167-2171).  Explicit contexts (sf_context_*) are for the
  *    batched and serving forms; one context must not be used by two threads
- *    at once.
+ *    at once.  Large batches are prepared on a pool of up to seven host
+ *    threads, started once per process.
+ *
+ * Environment (read when a plan is built; results never depend on them)
+ *  - SF_AFFINE16=0: every affine pass on the 32-bit rows (no packed 16-bit
+ *    rows).
+ *  - SF_AFFINE16_LANES=16: 16-bit passes on half warps by default (the
+ *    autotuner chooses per length bucket either way).
+ *  - SF_SORTED_CHAINS=1: the sorted entry points run the passes that can
+ *    share rows as chains (below, at sf_affine_sorted).
  */
 #ifndef SF_ALIGN_H
 #define SF_ALIGN_H
