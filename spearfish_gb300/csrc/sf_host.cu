@@ -213,8 +213,17 @@ struct BucketItem {
   uint64_t lat = 0;  // its warp's time, roughly: rows (steps) x the class's work per row
 };
 
+// Consecutive passes [first, first + count) of one sorted call that the chain kernel runs
+// as one chain, on class C.
+struct ChainSub {
+  size_t first;
+  uint32_t count;
+  int c;
+};
+
 // A plan's host-side build arrays, kept between builds: a rebuild of a similar batch reuses
-// their memory instead of faulting in fresh pages.
+// their memory instead of faulting in fresh pages.  The build's phases pass their results
+// to the next ones here.
 struct BuildScratch {
   std::vector<uint64_t> word_of, pass_work, pass_lat, tb_need, ops_need;
   std::vector<DJob> dj;
@@ -226,6 +235,12 @@ struct BuildScratch {
   std::vector<std::pair<BucketKey, BucketItem>> items, per;
   std::vector<uint8_t> has_item, seq_table;
   std::vector<std::pair<uint64_t, uint32_t>> byb;
+  std::vector<ChainSub> subs;
+  std::vector<DChain> chains;
+  std::vector<DLink> links;
+  std::vector<uint32_t> want;
+  uint64_t snap_words = 0;     // snapshot arena of the chains
+  uint64_t scratch_total = 0;  // wide buckets' scratch, all slices
 };
 
 }  // namespace sfe
@@ -339,15 +354,15 @@ void parallel_chunks(size_t n, size_t min_per_thread, int max_threads, F&& f) {
 }
 
 // Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
-int plan_build(sf_plan* P) {
-  using Key2 = BucketKey;
-  using Item = BucketItem;
-  if (!P->scratch) P->scratch.reset(new BuildScratch);
-  BuildScratch& S = *P->scratch;
-  sf_context* ctx = P->ctx;
-  CK(cudaSetDevice(ctx->dev));
+// The plan build, in phases: sequences, chains, pass descriptors, output offsets, chain
+// descriptors, buckets, upload, description.
+
+// Checks every pass's sequences against the pool (and the store), and lists the distinct
+// sequences with their packed word offsets: P->seq_* per distinct sequence, S.word_of[u]
+// per sequence u.
+int build_sequences(sf_plan* P, BuildScratch& S) {
+  const sf_context* ctx = P->ctx;
   const size_t np = P->passes.size();
-  if (np > 0xffffffffull / 2) return fail(SF_ERR_INVALID, "too many jobs");
   // Unique sequences.
   struct Key {
     uint64_t off;
@@ -504,34 +519,19 @@ int plan_build(sf_plan* P) {
     }
   }
   P->pool_words = words + 512;  // slack: kernels read whole windows past a sequence's end
+  return SF_OK;
+}
 
-  // Per-kind arrays.
-  auto& dj = S.dj;
-  auto& dp = S.dp;
-  auto& tj = S.tj;
-  auto& cls = S.cls;
-  auto& mj = S.mj;
-  auto& wlist = S.wlist;
-  wlist.clear();
-  P->slot.assign(np, 0);
-  auto& items = S.items;
-  items.clear();
-  items.reserve(np);
-  const bool use16 = allow16();
-  const int lanes16 = default_lanes16();
-  const TuneTable* tune = P->tune_override ? P->tune_override : &ctx->tune;
-  P->store = ctx->store;
-  // Sorted calls the chain kernel takes (Pass::chain on a call's first pass), when chains
-  // are on: every pass a 16-bit Global / Prefix pass without traceback, on the class of the
-  // call's widest row.  A call's passes form chains, each starting at a pass that resumes
-  // nothing (it depends on no earlier pass), which one warp runs in order.  Chains of one
-  // pass, and chains whose snapshots would pass the arena's cap, run as separate passes.
-  struct Sub {
-    size_t first;
-    uint32_t count;
-    int c;
-  };
-  std::vector<Sub> subs;
+// Sorted calls the chain kernel takes (Pass::chain on a call's first pass), when chains are
+// on: every pass a 16-bit Global / Prefix pass without traceback, on the class of the call's
+// widest row.  A call's passes form chains, each starting at a pass that resumes nothing (it
+// depends on no earlier pass), which one warp runs in order.  Chains of one pass, and chains
+// whose snapshots would pass the arena's cap, run as separate passes.  Fills S.subs and
+// P->chained.
+void choose_chains(sf_plan* P, BuildScratch& S, bool use16) {
+  const size_t np = P->passes.size();
+  auto& subs = S.subs;
+  subs.clear();
   P->chained.assign(np, 0);
   {
     constexpr uint64_t kSnapCapWords = (uint64_t(1) << 30) / 4;
@@ -566,7 +566,7 @@ int plan_build(sf_plan* P) {
         const uint64_t words = (e - h - 1) * snap_slot_words(c / 2);  // at most one per pass
         if (e - h >= 2 && snap_total + words <= kSnapCapWords) {
           snap_total += words;
-          subs.push_back(Sub{h, (uint32_t)(e - h), c});
+          subs.push_back(ChainSub{h, (uint32_t)(e - h), c});
           for (size_t u = h; u < e; ++u) P->chained[u] = 1;
         }
         h = e;
@@ -574,6 +574,24 @@ int plan_build(sf_plan* P) {
       q += cnt;
     }
   }
+}
+
+// Gives each pass its slot in its kind's arrays and writes its descriptor there, with its
+// bucket key and work item (S.per, S.has_item) unless a chain takes it.
+int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
+  using Key2 = BucketKey;
+  using Item = BucketItem;
+  const sf_context* ctx = P->ctx;
+  const size_t np = P->passes.size();
+  const int lanes16 = default_lanes16();
+  const TuneTable* tune = P->tune_override ? P->tune_override : &ctx->tune;
+  const auto& word_of = S.word_of;
+  auto& dj = S.dj;
+  auto& dp = S.dp;
+  auto& tj = S.tj;
+  auto& cls = S.cls;
+  auto& mj = S.mj;
+  P->slot.assign(np, 0);
   // Slots in each kind's arrays, in pass order.  Myers classes are checked here, so that the
   // parallel part below cannot fail.
   size_t n_myers = 0;
@@ -699,29 +717,52 @@ int plan_build(sf_plan* P) {
     }
   };
   parallel_chunks(np, 2048, kMaxThreads, describe);
-  // Offsets in pass order: traceback words, CIGAR slots, the walk list; then the items.
-  uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
+  uint64_t scratch_cells = 0;
   for (int w = 0; w < kMaxThreads; ++w) scratch_cells = std::max(scratch_cells, scratch_max[w]);
-  for (size_t sl = 0; sl < n_affine; ++sl) {
-    if (!(dp[sl].flags & F_TB)) continue;
+  P->scratch_cells = scratch_cells;
+  return SF_OK;
+}
+
+// Offsets in pass order: traceback words, CIGAR slots, the walk list; then the passes' work
+// items (S.items).
+void lay_out_outputs(sf_plan* P, BuildScratch& S) {
+  const size_t np = P->passes.size();
+  auto& dj = S.dj;
+  auto& tj = S.tj;
+  auto& wlist = S.wlist;
+  auto& items = S.items;
+  wlist.clear();
+  items.clear();
+  items.reserve(np);
+  uint64_t tb_words = 0, ops_words = 0;
+  for (size_t sl = 0; sl < dj.size(); ++sl) {
+    if (!(S.dp[sl].flags & F_TB)) continue;
     dj[sl].tb_word = tb_words;
-    tb_words += tb_need[sl];
+    tb_words += S.tb_need[sl];
     tj[sl].ops_off = ops_words;
-    ops_words += ops_need[sl];
+    ops_words += S.ops_need[sl];
     wlist.push_back((uint32_t)sl);
   }
   for (size_t q = 0; q < np; ++q)
-    if (has_item[q]) items.push_back(per[q]);
-  // Chains: one work item each (longest first, as passes); per chained job its link; per
-  // chain its snapshot rows, the sorted distinct resume rows (align.rs:2244-2246), and a
-  // slot for each.
-  std::vector<DChain> chains;
-  std::vector<DLink> links;
-  std::vector<uint32_t> want;
+    if (S.has_item[q]) items.push_back(S.per[q]);
+  P->tb_words = tb_words;
+  P->ops_words = ops_words;
+}
+
+// Chains: one work item each (longest first, as passes); per chained job its link; per
+// chain its snapshot rows, the sorted distinct resume rows (align.rs:2244-2246), and a slot
+// for each.
+void build_chains(sf_plan* P, BuildScratch& S) {
+  auto& chains = S.chains;
+  auto& links = S.links;
+  auto& want = S.want;
+  chains.clear();
+  links.clear();
+  want.clear();
   uint64_t snap_words = 0;
   uint32_t n_chained = 0;
-  for (const Sub& sb : subs) {
-    if (links.empty()) links.assign(dj.size(), DLink{});
+  for (const ChainSub& sb : S.subs) {
+    if (links.empty()) links.assign(S.dj.size(), DLink{});
     DChain ch{};
     ch.first = P->slot[sb.first];
     ch.count = sb.count;
@@ -731,8 +772,8 @@ int plan_build(sf_plan* P) {
     uint64_t work = 0, lat = 0;
     for (size_t u = sb.first; u < sb.first + sb.count; ++u) {
       if (u > sb.first) rows.push_back(P->passes[u].resume);
-      work += pass_work[u];
-      lat += pass_lat[u];
+      work += S.pass_work[u];
+      lat += S.pass_lat[u];
     }
     std::sort(rows.begin(), rows.end());
     rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
@@ -747,19 +788,22 @@ int plan_build(sf_plan* P) {
     }
     want.insert(want.end(), rows.begin(), rows.end());
     snap_words += rows.size() * snap_slot_words(sb.c / 2);
-    items.push_back({Key2{PK_CHAIN16, sb.c, 0, 0, 32}, Item{(uint32_t)chains.size(), work, lat}});
+    S.items.push_back({BucketKey{PK_CHAIN16, sb.c, 0, 0, 32},
+                       BucketItem{(uint32_t)chains.size(), work, lat}});
     chains.push_back(ch);
     n_chained += sb.count;
   }
+  S.snap_words = snap_words;
   P->n_chains = (uint32_t)chains.size();
   P->n_chained = n_chained;
-  P->n_aff = (uint32_t)dj.size();
-  P->n_my = (uint32_t)mj.size();
-  P->n_walk = (uint32_t)wlist.size();
-  P->tb_words = tb_words;
-  P->ops_words = ops_words;
-  P->scratch_cells = scratch_cells;
+}
 
+// Buckets of S.items by key, their launch order, shapes and streams (P->buckets), and the
+// execution order of the work items (S.order).
+void build_buckets(sf_plan* P, BuildScratch& S) {
+  using Key2 = BucketKey;
+  const sf_context* ctx = P->ctx;
+  const auto& items = S.items;
   // Buckets in key order; within a bucket, longest work first (ties in job order).  The
   // keys are few: a counting sort by bucket, then a sort by work inside each.
   std::vector<Key2> keys2;
@@ -882,14 +926,31 @@ int plan_build(sf_plan* P) {
       if (b.wide) {
         wide_warps += b.grid * 4;
         b.scratch_off = scratch_total;
-        scratch_total += (uint64_t)b.grid * 4 * 4 * scratch_cells;
+        scratch_total += (uint64_t)b.grid * 4 * 4 * P->scratch_cells;
       }
     }
   }
   P->wide_warps = wide_warps;
+  S.scratch_total = scratch_total;
   // Streams: round robin over the buckets in launch order, so that their tails overlap.
   for (size_t u = 0; u < P->buckets.size(); ++u) P->buckets[u].stream = (int)(u % sf_context::kAux);
-  // Device buffers.
+}
+
+// Device buffers sized for the plan, and its descriptors copied there.
+int upload_plan(sf_plan* P, BuildScratch& S) {
+  sf_context* ctx = P->ctx;
+  const auto& dj = S.dj;
+  const auto& dp = S.dp;
+  const auto& tj = S.tj;
+  const auto& cls = S.cls;
+  const auto& mj = S.mj;
+  const auto& wlist = S.wlist;
+  const auto& order = S.order;
+  const auto& chains = S.chains;
+  const auto& links = S.links;
+  const auto& want = S.want;
+  const uint64_t tb_words = P->tb_words, ops_words = P->ops_words;
+  const uint64_t scratch_total = S.scratch_total, snap_words = S.snap_words;
   int rc;
   if ((rc = P->d_bytes.ensure(std::max<uint64_t>(P->pool_bytes, 16)))) return rc;
   if ((rc = P->d_pool.ensure(P->pool_words * 4))) return rc;
@@ -966,7 +1027,11 @@ int plan_build(sf_plan* P) {
     P->graph = nullptr;
   }
   P->graph_tried = false;
-  // Description.
+  return SF_OK;
+}
+
+// The plan's description (sf_plan_describe): its buckets and arena sizes, as JSON.
+void describe_plan(sf_plan* P, const BuildScratch& S) {
   std::string d = "{\"buckets\": [";
   for (size_t q = 0; q < P->buckets.size(); ++q) {
     const Bucket& b = P->buckets[q];
@@ -986,11 +1051,33 @@ int plan_build(sf_plan* P) {
     d += buf;
   }
   d += "], \"chains\": " + std::to_string(P->n_chains) +
-       ", \"chained_passes\": " + std::to_string(n_chained) +
-       ", \"snapshot_bytes\": " + std::to_string(snap_words * 4) +
+       ", \"chained_passes\": " + std::to_string(P->n_chained) +
+       ", \"snapshot_bytes\": " + std::to_string(S.snap_words * 4) +
        ", \"pool_words\": " + std::to_string(P->pool_words) +
-       ", \"traceback_bytes\": " + std::to_string(tb_words * 4) + "}";
+       ", \"traceback_bytes\": " + std::to_string(P->tb_words * 4) + "}";
   P->desc = d;
+}
+
+int plan_build(sf_plan* P) {
+  if (!P->scratch) P->scratch.reset(new BuildScratch);
+  BuildScratch& S = *P->scratch;
+  sf_context* ctx = P->ctx;
+  CK(cudaSetDevice(ctx->dev));
+  if (P->passes.size() > 0xffffffffull / 2) return fail(SF_ERR_INVALID, "too many jobs");
+  int rc;
+  if ((rc = build_sequences(P, S))) return rc;
+  P->store = ctx->store;
+  const bool use16 = allow16();
+  choose_chains(P, S, use16);
+  if ((rc = describe_passes(P, S, use16))) return rc;
+  lay_out_outputs(P, S);
+  build_chains(P, S);
+  P->n_aff = (uint32_t)S.dj.size();
+  P->n_my = (uint32_t)S.mj.size();
+  P->n_walk = (uint32_t)S.wlist.size();
+  build_buckets(P, S);
+  if ((rc = upload_plan(P, S))) return rc;
+  describe_plan(P, S);
   return SF_OK;
 }
 
