@@ -195,6 +195,8 @@ struct sf_plan {
   std::vector<uint8_t> chained;
   // Pinned staging.
   PinBuf h_stage, h_res, h_mout, h_tres, h_ops, h_total;
+  // Recorded after the last copies out of h_stage (its next writer waits for it).
+  cudaEvent_t staged = nullptr;
   cudaGraphExec_t graph = nullptr;
   bool graph_tried = false;
   uint64_t launches = 0;

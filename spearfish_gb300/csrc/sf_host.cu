@@ -150,6 +150,16 @@ void apply_tune(const TuneTable* tune, int kind, int& c, bool wide, bool tb, int
   lanes = it->second.lanes;
 }
 
+// Whether choose_myers_class takes a pattern of m bases (a check that sets no error).
+bool myers_class_ok(uint32_t m) {
+  if (m > SF_MYERS_MAX_PATTERN) return false;
+  const uint32_t blocks = (m + 63) / 64;
+  if (blocks <= 32) return true;
+  for (int q = 0; q < sfk::kMyersNB; ++q)
+    if (32u * (uint32_t)sfk::kMyersB[q] >= blocks) return true;
+  return false;
+}
+
 int choose_myers_class(uint32_t m, int& b, int& lanes) {
   const uint32_t blocks = (m + 63) / 64;
   if (m > SF_MYERS_MAX_PATTERN) return fail(SF_ERR_TOO_LONG, "Myers pattern longer than SF_MYERS_MAX_PATTERN");
@@ -233,8 +243,9 @@ struct BuildScratch {
   std::vector<MJob> mj;
   std::vector<uint32_t> wlist, kid, order;
   std::vector<std::pair<BucketKey, BucketItem>> items, per;
-  std::vector<uint8_t> has_item, seq_table;
-  std::vector<std::pair<uint64_t, uint32_t>> byb;
+  std::vector<uint8_t> has_item;
+  std::vector<std::pair<uint64_t, uint32_t>> byb, byb_tmp;
+  std::vector<uint64_t> code_bits;
   std::vector<ChainSub> subs;
   std::vector<DChain> chains;
   std::vector<DLink> links;
@@ -249,6 +260,10 @@ sf_plan::sf_plan() = default;
 
 sf_plan::~sf_plan() {
   if (graph) cudaGraphExecDestroy(graph);
+  if (staged) {
+    cudaEventSynchronize(staged);  // copies out of h_stage end before it is freed
+    cudaEventDestroy(staged);
+  }
   if (owns_ctx) delete ctx;
 }
 
@@ -274,12 +289,17 @@ class HostPool {
     try {
       std::lock_guard<std::mutex> g(m_);
       q_.push_back(std::move(fn));
+      queued_.fetch_add(1, std::memory_order_release);
     } catch (...) {
       return false;
     }
     cv_.notify_one();
     return true;
   }
+  // How long a worker (or a caller waiting for its chunks) polls before it sleeps: a plan
+  // build posts its phases back to back, and a sleeping thread takes tens of microseconds
+  // to wake.
+  static constexpr std::chrono::microseconds kSpin{200};
 
  private:
   HostPool() : pid_(getpid()) {
@@ -293,12 +313,17 @@ class HostPool {
   }
   void loop() {
     for (;;) {
+      const auto t0 = std::chrono::steady_clock::now();
+      while (queued_.load(std::memory_order_acquire) == 0 &&
+             std::chrono::steady_clock::now() - t0 < kSpin) {
+      }
       std::function<void()> fn;
       {
         std::unique_lock<std::mutex> g(m_);
         cv_.wait(g, [this] { return !q_.empty(); });
         fn = std::move(q_.front());
         q_.pop_front();
+        queued_.fetch_sub(1, std::memory_order_relaxed);
       }
       fn();
     }
@@ -308,6 +333,7 @@ class HostPool {
   std::mutex m_;
   std::condition_variable cv_;
   std::deque<std::function<void()>> q_;
+  std::atomic<size_t> queued_{0};  // q_.size(), readable without the lock
 };
 
 // f(begin, end, k) for the k-th of up to max_threads contiguous chunks of [0, n), chunks 1..
@@ -324,36 +350,56 @@ void parallel_chunks(size_t n, size_t min_per_thread, int max_threads, F&& f) {
     return;
   }
   const size_t chunk = (n + t - 1) / t;
+  // `left` changes only under `m`, so that a worker is out of `done` once the caller has
+  // taken `m` after seeing it reach zero.
   struct Done {
     std::mutex m;
     std::condition_variable cv;
-    size_t left = 0;
+    std::atomic<size_t> left{0};
   } done;
   for (size_t k = 1; k < t; ++k) {
     const size_t b = k * chunk, e = std::min(n, (k + 1) * chunk);
     {
       std::lock_guard<std::mutex> g(done.m);
-      ++done.left;
+      done.left.fetch_add(1, std::memory_order_relaxed);
     }
     const bool queued = pool.post([&f, &done, b, e, k] {
       f(b, e, (int)k);
       std::lock_guard<std::mutex> g(done.m);
-      if (--done.left == 0) done.cv.notify_all();
+      if (done.left.fetch_sub(1, std::memory_order_acq_rel) == 1) done.cv.notify_all();
     });
     if (!queued) {
       {
         std::lock_guard<std::mutex> g(done.m);
-        --done.left;
+        done.left.fetch_sub(1, std::memory_order_relaxed);
       }
       f(b, e, (int)k);
     }
   }
   f(size_t(0), std::min(n, chunk), 0);
+  const auto t0 = std::chrono::steady_clock::now();
+  while (done.left.load(std::memory_order_acquire) != 0 &&
+         std::chrono::steady_clock::now() - t0 < HostPool::kSpin) {
+  }
   std::unique_lock<std::mutex> g(done.m);
-  done.cv.wait(g, [&] { return done.left == 0; });
+  done.cv.wait(g, [&] { return done.left.load(std::memory_order_acquire) == 0; });
 }
 
 // Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
+// h_stage holds data for asynchronous copies on the context's stream: stage_done marks the
+// end of the copies issued so far, and stage_wait waits for it before the staging is written
+// or reallocated again.
+int stage_wait(sf_plan* P) {
+  if (P->staged) CK(cudaEventSynchronize(P->staged));
+  return SF_OK;
+}
+
+int stage_done(sf_plan* P) {
+  if (!P->staged) CK(cudaEventCreateWithFlags(&P->staged, cudaEventDisableTiming));
+  CK(cudaEventRecord(P->staged, P->ctx->s));
+  return SF_OK;
+}
+
 // The plan build, in phases: sequences, chains, pass descriptors, output offsets, chain
 // descriptors, buckets, upload, description.
 
@@ -437,12 +483,6 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
   }
   auto& word_of = S.word_of;
   word_of.resize(2 * np);
-  P->seq_boff.clear();
-  P->seq_len.clear();
-  P->seq_woff.clear();
-  P->seq_boff.reserve(2 * np);
-  P->seq_len.reserve(2 * np);
-  P->seq_woff.reserve(2 * np);
   uint64_t words = 0;
   if (in_order) {
     // Two passes over chunks: count each chunk's new sequences and words, then write them
@@ -502,6 +542,9 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
       }
     });
   } else {
+    P->seq_boff.clear();
+    P->seq_len.clear();
+    P->seq_woff.clear();
     uint64_t last_off = 0;
     uint32_t last_len = 0;
     for (size_t q = 0; q < 2 * np; ++q) {
@@ -591,21 +634,39 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
   auto& tj = S.tj;
   auto& cls = S.cls;
   auto& mj = S.mj;
-  P->slot.assign(np, 0);
-  // Slots in each kind's arrays, in pass order.  Myers classes are checked here, so that the
-  // parallel part below cannot fail.
-  size_t n_myers = 0;
-  for (size_t q = 0; q < np; ++q) {
-    const Pass& p = P->passes[q];
-    if (p.kind == PK_MYERS) {
-      int b = 1, l = 1;
-      const int rc = choose_myers_class(p.m, b, l);
-      if (rc) return rc;
-      P->slot[q] = (uint32_t)n_myers++;
-    } else {
-      P->slot[q] = (uint32_t)(q - n_myers);
+  // Slots in each kind's arrays, in pass order: each chunk's Myers passes counted, then the
+  // slots written.  Myers classes are checked here, so that the parallel part below cannot
+  // fail.
+  constexpr int kT = 8;
+  uint64_t nmy[kT + 1] = {}, bad[kT];
+  for (int k = 0; k < kT; ++k) bad[k] = UINT64_MAX;
+  parallel_chunks(np, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t c = 0;
+    for (size_t q = q0; q < q1; ++q) {
+      const Pass& p = P->passes[q];
+      if (p.kind != PK_MYERS) continue;
+      if (!myers_class_ok(p.m)) {
+        bad[k] = q;
+        break;
+      }
+      ++c;
     }
+    nmy[k + 1] = c;
+  });
+  for (int k = 0; k < kT; ++k) {
+    if (bad[k] != UINT64_MAX) {
+      int b = 1, l = 1;
+      return choose_myers_class(P->passes[bad[k]].m, b, l);  // sets the error
+    }
+    nmy[k + 1] += nmy[k];
   }
+  P->slot.resize(np);
+  parallel_chunks(np, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t my = nmy[k];
+    for (size_t q = q0; q < q1; ++q)
+      P->slot[q] = (uint32_t)(P->passes[q].kind == PK_MYERS ? my++ : q - my);
+  });
+  const size_t n_myers = nmy[kT];
   const size_t n_affine = np - n_myers;
   mj.resize(n_myers);
   dj.resize(n_affine);
@@ -618,12 +679,13 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
   auto& ops_need = S.ops_need;
   auto& per = S.per;
   auto& has_item = S.has_item;
-  pass_work.assign(np, 0);
-  pass_lat.assign(np, 0);
-  tb_need.assign(n_affine, 0);
-  ops_need.assign(n_affine, 0);
+  // Every entry below is written for its pass by `describe`.
+  pass_work.resize(np);
+  pass_lat.resize(np);
+  tb_need.resize(n_affine);
+  ops_need.resize(n_affine);
   per.resize(np);
-  has_item.assign(np, 0);
+  has_item.resize(np);
   constexpr int kMaxThreads = 8;
   uint64_t scratch_max[kMaxThreads] = {};
   // Descriptors of passes [q0, q1), each written at its slot.
@@ -664,6 +726,7 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
         per[q] = {Key2{PK_MYERS, b, 0, 0, lanes},
                   Item{sl, (uint64_t)p.n, ((uint64_t)p.n + (uint64_t)lanes) * (4u * (uint64_t)b + 4u)}};
         has_item[q] = 1;
+        pass_work[q] = pass_lat[q] = 0;
         continue;
       }
       uint32_t flags = 0;
@@ -689,6 +752,8 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
         t.ops_cap = (uint32_t)std::min<uint64_t>(cap, 0xffffffffull);
         t.kind = p.tb_kind;
         t.end_bonus = p.end_bonus;
+      } else {
+        tb_need[sl] = ops_need[sl] = 0;
       }
       if (wide)
         scratch_max[worker] =
@@ -706,10 +771,8 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
       pass_work[q] = work;
       const uint64_t row_cost = (uint64_t)c * (wide ? (uint64_t)wide_chunks(c, wmax) : 1u) + 8u;
       pass_lat[q] = (uint64_t)std::max<uint32_t>(p.m, 1) * row_cost;
-      if (!P->chained[q]) {
-        per[q] = {Key2{kind, c, wide, tb, ln}, Item{sl, work, pass_lat[q]}};
-        has_item[q] = 1;
-      }
+      has_item[q] = !P->chained[q];
+      if (has_item[q]) per[q] = {Key2{kind, c, wide, tb, ln}, Item{sl, work, pass_lat[q]}};
       dj[sl] = j;
       dp[sl] = pr;
       tj[sl] = t;
@@ -726,27 +789,58 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
 // Offsets in pass order: traceback words, CIGAR slots, the walk list; then the passes' work
 // items (S.items).
 void lay_out_outputs(sf_plan* P, BuildScratch& S) {
-  const size_t np = P->passes.size();
+  const size_t np = P->passes.size(), na = S.dj.size();
   auto& dj = S.dj;
   auto& tj = S.tj;
   auto& wlist = S.wlist;
   auto& items = S.items;
-  wlist.clear();
-  items.clear();
-  items.reserve(np);
-  uint64_t tb_words = 0, ops_words = 0;
-  for (size_t sl = 0; sl < dj.size(); ++sl) {
-    if (!(S.dp[sl].flags & F_TB)) continue;
-    dj[sl].tb_word = tb_words;
-    tb_words += S.tb_need[sl];
-    tj[sl].ops_off = ops_words;
-    ops_words += S.ops_need[sl];
-    wlist.push_back((uint32_t)sl);
+  // Two passes over the same chunks: each chunk's totals, then its entries at their places.
+  constexpr int kT = 8;
+  struct Sums {
+    uint64_t tb = 0, ops = 0, walks = 0;
+  } sum[kT + 1];
+  parallel_chunks(na, 4096, kT, [&](size_t s0, size_t s1, int k) {
+    Sums z;
+    for (size_t sl = s0; sl < s1; ++sl) {
+      if (!(S.dp[sl].flags & F_TB)) continue;
+      z.tb += S.tb_need[sl];
+      z.ops += S.ops_need[sl];
+      z.walks++;
+    }
+    sum[k + 1] = z;
+  });
+  for (int k = 0; k < kT; ++k) {
+    sum[k + 1].tb += sum[k].tb;
+    sum[k + 1].ops += sum[k].ops;
+    sum[k + 1].walks += sum[k].walks;
   }
-  for (size_t q = 0; q < np; ++q)
-    if (S.has_item[q]) items.push_back(S.per[q]);
-  P->tb_words = tb_words;
-  P->ops_words = ops_words;
+  wlist.resize(sum[kT].walks);
+  parallel_chunks(na, 4096, kT, [&](size_t s0, size_t s1, int k) {
+    Sums z = sum[k];
+    for (size_t sl = s0; sl < s1; ++sl) {
+      if (!(S.dp[sl].flags & F_TB)) continue;
+      dj[sl].tb_word = z.tb;
+      z.tb += S.tb_need[sl];
+      tj[sl].ops_off = z.ops;
+      z.ops += S.ops_need[sl];
+      wlist[z.walks++] = (uint32_t)sl;
+    }
+  });
+  uint64_t cnt[kT + 1] = {};
+  parallel_chunks(np, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t c = 0;
+    for (size_t q = q0; q < q1; ++q) c += S.has_item[q];
+    cnt[k + 1] = c;
+  });
+  for (int k = 0; k < kT; ++k) cnt[k + 1] += cnt[k];
+  items.resize(cnt[kT]);
+  parallel_chunks(np, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t at = cnt[k];
+    for (size_t q = q0; q < q1; ++q)
+      if (S.has_item[q]) items[at++] = S.per[q];
+  });
+  P->tb_words = sum[kT].tb;
+  P->ops_words = sum[kT].ops;
 }
 
 // Chains: one work item each (longest first, as passes); per chained job its link; per
@@ -804,98 +898,170 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
   using Key2 = BucketKey;
   const sf_context* ctx = P->ctx;
   const auto& items = S.items;
-  // Buckets in key order; within a bucket, longest work first (ties in job order).  The
-  // keys are few: a counting sort by bucket, then a sort by work inside each.
-  std::vector<Key2> keys2;
+  const size_t ni = items.size();
+  constexpr int kT = 8;
+  // Buckets in key order; within a bucket, longest work first (ties in job order).
+  // Each item's bucket first: keys pack into 18-bit codes ordered as the keys are (kind < 8,
+  // C < 128, lanes < 64), so a bit set of the codes present lists the buckets in order and a
+  // code's bucket is the number of codes below it.  Keys outside those bounds (never built)
+  // take a search instead.
   auto& kid = S.kid;
-  kid.resize(items.size());
+  kid.resize(ni);
+  std::vector<Key2> keys;  // the buckets' keys, in order
   {
-    // A key packs into 18 bits (kind < 8, C < 128, lanes <= 32): a direct table of key
-    // indices, reset after use.
-    static thread_local std::vector<int32_t> index_of(1u << 18, -1);
-    auto code = [](const Key2& k) {
-      return ((uint32_t)k.kind & 7u) << 15 | ((uint32_t)k.c & 127u) << 8 |
-             ((uint32_t)k.wide & 1u) << 7 | ((uint32_t)k.tb & 1u) << 6 |
-             ((uint32_t)k.lanes & 63u);
+    constexpr uint32_t kWords = (1u << 18) / 64;
+    auto fits = [](const Key2& k) {
+      return k.kind >= 0 && k.kind < 8 && k.c >= 0 && k.c < 128 && (k.wide & ~1) == 0 &&
+             (k.tb & ~1) == 0 && k.lanes >= 0 && k.lanes < 64;
     };
-    for (size_t q = 0; q < items.size(); ++q) {
-      const Key2& k = items[q].first;
-      int32_t& at = index_of[code(k)];
-      if (at < 0 || !(keys2[(size_t)at] == k)) {
-        // A code is unique per key within the bounds above; a key outside them (never
-        // built) falls back to a search.
-        int32_t f = -1;
-        for (size_t u = 0; u < keys2.size(); ++u)
-          if (keys2[u] == k) f = (int32_t)u;
-        if (f < 0) {
-          keys2.push_back(k);
-          f = (int32_t)keys2.size() - 1;
+    auto& bits = S.code_bits;
+    bits.assign((size_t)kT * kWords, 0);
+    bool packed[kT];
+    std::fill(packed, packed + kT, true);
+    parallel_chunks(ni, 4096, kT, [&](size_t q0, size_t q1, int k) {
+      uint64_t* w = bits.data() + (size_t)k * kWords;
+      for (size_t q = q0; q < q1; ++q) {
+        const Key2& key = items[q].first;
+        if (!fits(key)) {
+          packed[k] = false;
+          return;
         }
-        if (at < 0) at = f;
-        kid[q] = (uint32_t)f;
-        continue;
+        const uint32_t c = (uint32_t)key.kind << 15 | (uint32_t)key.c << 8 |
+                           (uint32_t)key.wide << 7 | (uint32_t)key.tb << 6 | (uint32_t)key.lanes;
+        kid[q] = c;
+        w[c >> 6] |= uint64_t(1) << (c & 63);
       }
-      kid[q] = (uint32_t)at;
+    });
+    if (std::all_of(packed, packed + kT, [](bool x) { return x; })) {
+      std::vector<uint32_t> below(kWords + 1, 0);
+      for (uint32_t w = 0; w < kWords; ++w) {
+        uint64_t x = 0;
+        for (int k = 0; k < kT; ++k) x |= bits[(size_t)k * kWords + w];
+        bits[w] = x;
+        below[w + 1] = below[w] + (uint32_t)__builtin_popcountll(x);
+        for (; x; x &= x - 1) {
+          const int c = (int)(w * 64 + (uint32_t)__builtin_ctzll(x));
+          keys.push_back(Key2{c >> 15, (c >> 8) & 127, (c >> 7) & 1, (c >> 6) & 1, c & 63});
+        }
+      }
+      parallel_chunks(ni, 4096, kT, [&](size_t q0, size_t q1, int) {
+        for (size_t q = q0; q < q1; ++q) {
+          const uint32_t c = kid[q];
+          kid[q] = below[c >> 6] + (uint32_t)__builtin_popcountll(bits[c >> 6] & ((uint64_t(1) << (c & 63)) - 1));
+        }
+      });
+    } else {
+      for (const auto& it : items) keys.push_back(it.first);
+      std::sort(keys.begin(), keys.end());
+      keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+      for (size_t q = 0; q < ni; ++q)
+        kid[q] = (uint32_t)(std::lower_bound(keys.begin(), keys.end(), items[q].first) - keys.begin());
     }
-    for (const Key2& k : keys2) index_of[code(k)] = -1;
   }
-  std::vector<uint32_t> rank(keys2.size());
+  // A stable counting sort by bucket: each chunk's items and work per bucket, then the
+  // chunks' places (bucket-major, chunk-minor) and a second pass over the same chunks.
+  const size_t nb = keys.size();
+  std::vector<uint64_t> at((size_t)kT * nb, 0), wsum((size_t)kT * nb, 0);
+  parallel_chunks(ni, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t* c = at.data() + (size_t)k * nb;
+    uint64_t* ws = wsum.data() + (size_t)k * nb;
+    for (size_t q = q0; q < q1; ++q) {
+      c[kid[q]]++;
+      ws[kid[q]] += items[q].second.work;
+    }
+  });
+  std::vector<uint64_t> start(nb + 1, 0), bwork(nb, 0);
   {
-    std::vector<uint32_t> idx(keys2.size());
-    for (size_t u = 0; u < idx.size(); ++u) idx[u] = (uint32_t)u;
-    std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return keys2[a] < keys2[b]; });
-    for (size_t u = 0; u < idx.size(); ++u) rank[idx[u]] = (uint32_t)u;
+    uint64_t acc = 0;
+    for (size_t u = 0; u < nb; ++u) {
+      start[u] = acc;
+      for (int k = 0; k < kT; ++k) {
+        const uint64_t c = at[(size_t)k * nb + u];
+        at[(size_t)k * nb + u] = acc;
+        acc += c;
+        bwork[u] += wsum[(size_t)k * nb + u];
+      }
+    }
+    start[nb] = acc;
   }
-  std::vector<uint64_t> start(keys2.size() + 1, 0), bwork(keys2.size(), 0);
-  for (size_t q = 0; q < items.size(); ++q) {
-    start[rank[kid[q]] + 1]++;
-    bwork[kid[q]] += items[q].second.work;
-  }
-  for (size_t u = 0; u < keys2.size(); ++u) start[u + 1] += start[u];
   auto& byb = S.byb;  // (work, job order) by bucket
-  byb.resize(items.size());
-  {
-    std::vector<uint64_t> at(start.begin(), start.end() - 1);
-    for (size_t q = 0; q < items.size(); ++q) byb[at[rank[kid[q]]]++] = {items[q].second.work, (uint32_t)q};
-  }
+  byb.resize(ni);
+  parallel_chunks(ni, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t* a = at.data() + (size_t)k * nb;
+    for (size_t q = q0; q < q1; ++q) byb[a[kid[q]]++] = {items[q].second.work, (uint32_t)q};
+  });
   auto& order = S.order;
-  order.resize(items.size());
-  P->buckets.clear();
-  std::vector<Key2> sorted_keys(keys2.size());
-  for (size_t u = 0; u < keys2.size(); ++u) sorted_keys[rank[u]] = keys2[u];
-  std::vector<uint64_t> bw(keys2.size());
-  for (size_t u = 0; u < keys2.size(); ++u) bw[rank[u]] = bwork[u];
-  bwork.swap(bw);
+  order.resize(ni);
+  P->buckets.assign(nb, Bucket{});
+  for (size_t u = 0; u < nb; ++u) {
+    Bucket& b = P->buckets[u];
+    b.kind = (PassKind)keys[u].kind;
+    b.c = keys[u].c;
+    b.wide = keys[u].wide;
+    b.tb = keys[u].tb;
+    b.lanes = keys[u].lanes;
+    b.first = (uint32_t)start[u];
+    b.count = (uint32_t)(start[u + 1] - start[u]);
+    b.work = bwork[u];
+  }
   // Longest first within a bucket, by work rounded to 1/16 of its power of two (a stable
-  // counting sort: equal rounded work keeps job order).
+  // counting sort: equal rounded work keeps job order).  Buckets of many items sort on the
+  // host pool one at a time; the others sort side by side.
   auto wbin = [](uint64_t w) -> uint32_t {
     if (w < 16) return (uint32_t)w;
     const int e = 63 - __builtin_clzll(w);  // w in [2^e, 2^(e+1))
     return (uint32_t)(16 * (e - 3) + ((w >> (e - 4)) & 15));
   };
   constexpr uint32_t kBins = 16 * 61 + 16;
-  // Buckets sort their items independently: on the host pool for large batches.
-  P->buckets.assign(sorted_keys.size(), Bucket{});
-  parallel_chunks(sorted_keys.size(), items.size() >= 16384 ? 1 : sorted_keys.size() + 1, 8,
-                  [&](size_t u0, size_t u1, int) {
-    std::vector<uint32_t> bin_at(kBins + 1);
-    std::vector<std::pair<uint64_t, uint32_t>> tmp;
+  constexpr size_t kBig = 16384;
+  auto& tmp = S.byb_tmp;
+  std::vector<uint64_t> bin_at((size_t)kT * kBins);
+  for (size_t u = 0; u < nb; ++u) {
+    Bucket& b = P->buckets[u];
+    if (b.count < kBig) continue;
+    const auto* src = byb.data() + b.first;
+    const size_t n = b.count;
+    std::fill(bin_at.begin(), bin_at.end(), 0);
+    parallel_chunks(n, 4096, kT, [&](size_t e0, size_t e1, int k) {
+      uint64_t* c = bin_at.data() + (size_t)k * kBins;
+      for (size_t e = e0; e < e1; ++e) c[kBins - 1 - wbin(src[e].first)]++;
+    });
+    uint64_t acc = 0;
+    for (uint32_t v = 0; v < kBins; ++v)
+      for (int k = 0; k < kT; ++k) {
+        const uint64_t c = bin_at[(size_t)k * kBins + v];
+        bin_at[(size_t)k * kBins + v] = acc;
+        acc += c;
+      }
+    tmp.resize(n);
+    parallel_chunks(n, 4096, kT, [&](size_t e0, size_t e1, int k) {
+      uint64_t* a = bin_at.data() + (size_t)k * kBins;
+      for (size_t e = e0; e < e1; ++e) tmp[a[kBins - 1 - wbin(src[e].first)]++] = src[e];
+    });
+    uint64_t lat[kT] = {};
+    parallel_chunks(n, 4096, kT, [&](size_t e0, size_t e1, int k) {
+      uint64_t l = 0;
+      for (size_t e = e0; e < e1; ++e) {
+        const BucketItem& it = items[tmp[e].second].second;
+        order[b.first + e] = it.slot;
+        l = std::max(l, it.lat);
+      }
+      lat[k] = l;
+    });
+    b.lat = *std::max_element(lat, lat + kT);
+  }
+  parallel_chunks(nb, ni >= kBig ? 1 : nb + 1, kT, [&](size_t u0, size_t u1, int) {
+    std::vector<uint32_t> bin_n(kBins + 1);
+    std::vector<std::pair<uint64_t, uint32_t>> part;
     for (size_t u = u0; u < u1; ++u) {
-      auto b0 = byb.begin() + (ptrdiff_t)start[u], b1 = byb.begin() + (ptrdiff_t)start[u + 1];
-      std::fill(bin_at.begin(), bin_at.end(), 0u);
-      for (auto it = b0; it != b1; ++it) bin_at[kBins - 1 - wbin(it->first) + 1]++;
-      for (uint32_t k = 0; k < kBins; ++k) bin_at[k + 1] += bin_at[k];
-      tmp.assign(b0, b1);
-      for (const auto& e : tmp) *(b0 + bin_at[kBins - 1 - wbin(e.first)]++) = e;
       Bucket& b = P->buckets[u];
-      b.kind = (PassKind)sorted_keys[u].kind;
-      b.c = sorted_keys[u].c;
-      b.wide = sorted_keys[u].wide;
-      b.tb = sorted_keys[u].tb;
-      b.lanes = sorted_keys[u].lanes;
-      b.first = (uint32_t)start[u];
-      b.count = (uint32_t)(start[u + 1] - start[u]);
-      b.work = bwork[u];
+      if (b.count >= kBig) continue;
+      auto b0 = byb.begin() + (ptrdiff_t)b.first, b1 = b0 + (ptrdiff_t)b.count;
+      std::fill(bin_n.begin(), bin_n.end(), 0u);
+      for (auto it = b0; it != b1; ++it) bin_n[kBins - 1 - wbin(it->first) + 1]++;
+      for (uint32_t k = 0; k < kBins; ++k) bin_n[k + 1] += bin_n[k];
+      part.assign(b0, b1);
+      for (const auto& e : part) *(b0 + bin_n[kBins - 1 - wbin(e.first)]++) = e;
       for (auto it = b0; it != b1; ++it) {
         order[(size_t)(it - byb.begin())] = items[it->second].second.slot;
         b.lat = std::max(b.lat, items[it->second].second.lat);
@@ -977,51 +1143,63 @@ int upload_plan(sf_plan* P, BuildScratch& S) {
   if ((rc = P->d_links.ensure(links.size() * sizeof(DLink) + 64))) return rc;
   if ((rc = P->d_want.ensure(want.size() * 4 + 64))) return rc;
   if ((rc = P->d_snap.ensure(snap_words * 4 + 64))) return rc;
-  // Descriptors -> device (one pinned staging area, one stream).
-  const size_t seq_bytes = nseq * 20;
-  const size_t total = seq_bytes + dj.size() * (sizeof(DJob) + sizeof(DParams) + sizeof(TJob) + 1) +
-                       mj.size() * sizeof(MJob) + order.size() * 4 + wlist.size() * 4 +
-                       chains.size() * sizeof(DChain) + links.size() * sizeof(DLink) +
-                       want.size() * 4 + 1024;
-  if ((rc = P->h_stage.ensure(total))) return rc;
-  uint8_t* h = P->h_stage.as<uint8_t>();
-  size_t at = 0;
-  auto put = [&](DevBuf& d, const void* src, size_t bytes) -> int {
-    if (!bytes) return SF_OK;
-    // Large descriptor arrays are copied into the pinned staging on host threads.
-    constexpr size_t kPiece = size_t(1) << 20;
-    uint8_t* dst = h + at;
-    const uint8_t* from = static_cast<const uint8_t*>(src);
-    parallel_chunks((bytes + kPiece - 1) / kPiece, 2, 8, [&](size_t k0, size_t k1, int) {
-      const size_t b0 = k0 * kPiece, b1 = std::min(bytes, k1 * kPiece);
-      if (b1 > b0) std::memcpy(dst + b0, from + b0, b1 - b0);
-    });
-    cudaError_t e = cudaMemcpyAsync(d.p, h + at, bytes, cudaMemcpyHostToDevice, ctx->s);
-    at += (bytes + 15) & ~size_t(15);
-    return e == cudaSuccess ? SF_OK : fail(SF_ERR_CUDA, cudaGetErrorString(e));
+  // Descriptors -> device (one pinned staging area, one stream).  Every array goes into the
+  // staging (on host threads, in pieces), then one copy per device buffer.  The sequence
+  // table is byte offsets, word offsets (both 8-byte aligned), then lengths.
+  struct Part {
+    const void* src;
+    size_t bytes, at;
   };
+  struct Copy {
+    DevBuf* d;
+    size_t at, bytes;
+  };
+  std::vector<Part> parts;
+  std::vector<Copy> copies;
+  size_t at = 0;
+  auto put = [&](DevBuf& d, std::initializer_list<std::pair<const void*, size_t>> srcs) {
+    size_t bytes = 0;
+    for (const auto& sp : srcs) {
+      if (sp.second) parts.push_back(Part{sp.first, sp.second, at + bytes});
+      bytes += sp.second;
+    }
+    if (!bytes) return;
+    copies.push_back(Copy{&d, at, bytes});
+    at += (bytes + 15) & ~size_t(15);
+  };
+  put(P->d_seq, {{P->seq_boff.data(), nseq * 8}, {P->seq_woff.data(), nseq * 8},
+                 {P->seq_len.data(), nseq * 4}});
+  put(P->d_djobs, {{dj.data(), dj.size() * sizeof(DJob)}});
+  put(P->d_params, {{dp.data(), dp.size() * sizeof(DParams)}});
+  put(P->d_tjobs, {{tj.data(), tj.size() * sizeof(TJob)}});
+  put(P->d_cls, {{cls.data(), cls.size() * 2}});
+  put(P->d_mjobs, {{mj.data(), mj.size() * sizeof(MJob)}});
+  put(P->d_order, {{order.data(), order.size() * 4}});
+  put(P->d_wlist, {{wlist.data(), wlist.size() * 4}});
+  put(P->d_chains, {{chains.data(), chains.size() * sizeof(DChain)}});
+  put(P->d_links, {{links.data(), links.size() * sizeof(DLink)}});
+  put(P->d_want, {{want.data(), want.size() * 4}});
+  if ((rc = stage_wait(P))) return rc;
+  if ((rc = P->h_stage.ensure(at + 16))) return rc;
+  uint8_t* h = P->h_stage.as<uint8_t>();
   {
-    // Sequence table: byte offsets, word offsets (both 8-byte aligned), then lengths.
-    auto& st = S.seq_table;
-    st.resize(seq_bytes);
-    std::memcpy(st.data(), P->seq_boff.data(), nseq * 8);
-    std::memcpy(st.data() + nseq * 8, P->seq_woff.data(), nseq * 8);
-    std::memcpy(st.data() + nseq * 16, P->seq_len.data(), nseq * 4);
-    if ((rc = put(P->d_seq, st.data(), seq_bytes))) return rc;
+    constexpr size_t kPiece = size_t(256) << 10;
+    std::vector<std::pair<uint32_t, size_t>> pieces;  // (part, offset)
+    for (size_t u = 0; u < parts.size(); ++u)
+      for (size_t o = 0; o < parts[u].bytes; o += kPiece) pieces.push_back({(uint32_t)u, o});
+    parallel_chunks(pieces.size(), 2, 8, [&](size_t k0, size_t k1, int) {
+      for (size_t k = k0; k < k1; ++k) {
+        const Part& pt = parts[pieces[k].first];
+        const size_t o = pieces[k].second, n = std::min(kPiece, pt.bytes - o);
+        std::memcpy(h + pt.at + o, static_cast<const uint8_t*>(pt.src) + o, n);
+      }
+    });
   }
-  if ((rc = put(P->d_djobs, dj.data(), dj.size() * sizeof(DJob)))) return rc;
-  if ((rc = put(P->d_params, dp.data(), dp.size() * sizeof(DParams)))) return rc;
-  if ((rc = put(P->d_tjobs, tj.data(), tj.size() * sizeof(TJob)))) return rc;
-  if ((rc = put(P->d_cls, cls.data(), cls.size() * 2))) return rc;
-  if ((rc = put(P->d_mjobs, mj.data(), mj.size() * sizeof(MJob)))) return rc;
-  if ((rc = put(P->d_order, order.data(), order.size() * 4))) return rc;
-  if ((rc = put(P->d_wlist, wlist.data(), wlist.size() * 4))) return rc;
-  if ((rc = put(P->d_chains, chains.data(), chains.size() * sizeof(DChain)))) return rc;
-  if ((rc = put(P->d_links, links.data(), links.size() * sizeof(DLink)))) return rc;
-  if ((rc = put(P->d_want, want.data(), want.size() * 4))) return rc;
+  for (const Copy& c : copies)
+    CK(cudaMemcpyAsync(c.d->p, h + c.at, c.bytes, cudaMemcpyHostToDevice, ctx->s));
   // The pool's slack words stay zero.
   CK(cudaMemsetAsync(P->d_pool.p, 0, P->pool_words * 4, ctx->s));
-  CK(cudaStreamSynchronize(ctx->s));  // staging is reused by the next upload
+  if ((rc = stage_done(P))) return rc;
   if (P->graph) {
     cudaGraphExecDestroy(P->graph);
     P->graph = nullptr;
@@ -1321,6 +1499,8 @@ int run_passes(std::vector<Pass>& passes, const Gather& g, std::vector<DRes>* re
   if ((rc = plan_build(P))) return rc;
   // Pool: gather into pinned staging, then one copy.
   if (g.bytes) {
+    // The staging is the build's too: its descriptor copies end first.
+    if ((rc = stage_wait(P))) return rc;
     if ((rc = P->h_stage.ensure(g.bytes))) return rc;
     uint8_t* h = P->h_stage.as<uint8_t>();
     uint64_t at = 0;
@@ -1329,6 +1509,7 @@ int run_passes(std::vector<Pass>& passes, const Gather& g, std::vector<DRes>* re
       at += pr.second;
     }
     CK(cudaMemcpyAsync(P->d_bytes.p, h, g.bytes, cudaMemcpyHostToDevice, P->ctx->s));
+    if ((rc = stage_done(P))) return rc;
   }
   if ((rc = plan_execute(P, false))) return rc;
   if ((rc = plan_fetch(P))) return rc;
@@ -1560,7 +1741,15 @@ int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_c
   const TRes* tr = P->h_tres.as<TRes>();
   const uint32_t* mo = P->h_mout.as<uint32_t>();
   const size_t np = P->passes.size();
-  parallel_chunks(np, 2048, 8, [&](size_t q0, size_t q1, int) {
+  // Compacted op order = walk-list order = pass order among CIGAR passes: each chunk's ops
+  // counted while its results convert, then its passes' offsets.
+  constexpr int kT = 8;
+  uint64_t ops_of[kT + 1] = {};
+  auto has_ops = [](const Pass& p) {
+    return p.want_cigar && p.kind != PK_LOCAL && p.kind != PK_MYERS;
+  };
+  parallel_chunks(np, 2048, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t n_ops = 0;
     for (size_t q = q0; q < q1; ++q) {
       const Pass& p = P->passes[q];
       sf_result_t& o = results[q];
@@ -1599,17 +1788,20 @@ int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_c
         o.status = t.status;
         o.text_start = t.text_start;
         o.n_ops = t.status == 0 ? t.n_ops : 0;
+        n_ops += o.n_ops;
       }
     }
+    ops_of[k + 1] = n_ops;
   });
-  // Compacted op order = walk-list order = pass order among CIGAR passes.
-  uint64_t acc = 0;
-  for (size_t q = 0; q < np; ++q) {
-    const Pass& p = P->passes[q];
-    if (!p.want_cigar || p.kind == PK_LOCAL || p.kind == PK_MYERS) continue;
-    results[q].cigar_off = acc;
-    acc += results[q].n_ops;
-  }
+  for (int k = 0; k < kT; ++k) ops_of[k + 1] += ops_of[k];
+  parallel_chunks(np, 2048, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t acc = ops_of[k];
+    for (size_t q = q0; q < q1; ++q) {
+      if (!has_ops(P->passes[q])) continue;
+      results[q].cigar_off = acc;
+      acc += results[q].n_ops;
+    }
+  });
   return SF_OK;
 }
 
