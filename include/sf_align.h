@@ -33,6 +33,8 @@
  *    autotuner chooses per length bucket either way).
  *  - SF_SORTED_CHAINS=1: the sorted entry points run the passes that can
  *    share rows as chains (below, at sf_affine_sorted).
+ *  - SF_BATCH_SEGMENTS=0: sf_batch_run builds every batch as one plan (no
+ *    segments, below).
  */
 #ifndef SF_ALIGN_H
 #define SF_ALIGN_H
@@ -302,7 +304,11 @@ int sf_plan_tune(sf_plan *plan, const uint8_t *pool, uint32_t reps, char *report
 int sf_context_untune(sf_context *ctx);
 
 /* One call on the context's reusable plan: descriptors, upload, execute,
- * download (buffers grow and are reused across calls). */
+ * download (buffers grow and are reused across calls).  A batch of at least
+ * 8,192 jobs whose jobs are of similar work (none above 8x the mean) runs in
+ * up to four segments of consecutive jobs, each its own plan: the host
+ * prepares segment k + 1 while the device runs segment k.  Results, CIGAR
+ * ops and their order (job order) are the same either way. */
 int sf_batch_run(sf_context *ctx, const uint8_t *pool, uint64_t pool_bytes,
                  const sf_job_t *jobs, uint64_t count,
                  const sf_affine_t *scores, uint32_t n_scores,

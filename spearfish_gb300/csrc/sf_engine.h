@@ -197,6 +197,9 @@ struct sf_plan {
   PinBuf h_stage, h_res, h_mout, h_tres, h_ops, h_total;
   // Recorded after the last copies out of h_stage (its next writer waits for it).
   cudaEvent_t staged = nullptr;
+  // The device byte pool of another plan this one reads instead of its own d_bytes (the
+  // later segments of a segmented batch), or null.
+  const uint8_t* bytes_from = nullptr;
   cudaGraphExec_t graph = nullptr;
   bool graph_tried = false;
   uint64_t launches = 0;
@@ -237,9 +240,13 @@ struct sf_context {
   cudaStream_t aux[kAux] = {};
   cudaEvent_t fork = nullptr, join[kAux] = {};
   std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
+  // sf_batch_run's later segments of a large batch (the first is `cache`).
+  static constexpr int kSegs = 4;
+  std::unique_ptr<sf_plan> segs[kSegs - 1];
   sfe::TuneTable tune;             // autotuner choices, applied to every later plan
   sf_store* store = nullptr;       // transcript store for SF_TEXT_STORE texts
   ~sf_context() {
+    for (auto& p : segs) p.reset();
     cache.reset();
     int prev = 0;
     cudaGetDevice(&prev);
@@ -268,8 +275,9 @@ int plan_execute(sf_plan* P, bool use_graph);
 int plan_fetch(sf_plan* P);
 int plan_fetch_ops(sf_plan* P, uint64_t& total);
 // Converts a fetched plan's results to sf_result_t (and copies compacted ops).
+// `ops_base` is added to every cigar_off (the ops of earlier segments before `ops`).
 int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
-                 uint64_t total, bool copy_ops = true);
+                 uint64_t total, bool copy_ops = true, uint64_t ops_base = 0);
 // Device bytes a plan of these passes needs (upper bound, before building it).
 uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_bytes);
 // Device bytes the plan's buffers hold now.

@@ -110,6 +110,12 @@ int default_lanes16() {
 // the passes of a sorted call that can share rows as chains; by default every pass runs
 // separately (the results are the same either way, and separate passes finish sooner on the
 // batches measured: a chain runs its passes one after another); read once per plan.
+// Large sf_batch_run batches run in segments (SF_BATCH_SEGMENTS=0 turns it off).
+bool batch_segments_on() {
+  const char* e = std::getenv("SF_BATCH_SEGMENTS");
+  return !(e && e[0] == '0');
+}
+
 bool allow_chains() {
   const char* env = std::getenv("SF_SORTED_CHAINS");
   return env && env[0] == '1';
@@ -424,6 +430,10 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
   };
   constexpr int kChunks = 8;
   bool in_order = true;
+  // Per chunk of passes (the same chunks below): its new sequences and their words, counted
+  // as if the pool were in order (a sequence equal to the one before it shares its words).
+  size_t cnt[kChunks] = {};
+  uint64_t wsum[kChunks] = {};
   {
     auto bad_pass = [&](const Pass& p) {
       return (p.p_off & kOffMask) + p.m > P->pool_bytes ||
@@ -450,6 +460,10 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
           uint32_t l;
           seq_of(2 * q + h, o, l);
           if (q + h > 0 && (o < po || (o == po && l < pl))) ordered[k] = false;
+          if (q + h == 0 || o != po || l != pl) {
+            cnt[k]++;
+            wsum[k] += seq_words(l);
+          }
           po = o;
           pl = l;
         }
@@ -485,27 +499,9 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
   word_of.resize(2 * np);
   uint64_t words = 0;
   if (in_order) {
-    // Two passes over chunks: count each chunk's new sequences and words, then write them
-    // at their places (a sequence equal to the one before it shares its words).
-    const size_t ns = 2 * np;
-    size_t cnt[kChunks] = {}, at0[kChunks] = {};
-    uint64_t wsum[kChunks] = {}, w0[kChunks] = {};
-    parallel_chunks(ns, 4096, kChunks, [&](size_t u0, size_t u1, int k) {
-      uint64_t po = 0;
-      uint32_t pl = 0;
-      if (u0 > 0) seq_of(u0 - 1, po, pl);
-      for (size_t u = u0; u < u1; ++u) {
-        uint64_t o;
-        uint32_t l;
-        seq_of(u, o, l);
-        if (u == 0 || o != po || l != pl) {
-          cnt[k]++;
-          wsum[k] += seq_words(l);
-        }
-        po = o;
-        pl = l;
-      }
-    });
+    // Each chunk's new sequences at their places, from the counts above.
+    size_t at0[kChunks] = {};
+    uint64_t w0[kChunks] = {};
     size_t total = 0;
     for (int k = 0; k < kChunks; ++k) {
       at0[k] = total;
@@ -516,7 +512,8 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
     P->seq_boff.resize(total);
     P->seq_len.resize(total);
     P->seq_woff.resize(total);
-    parallel_chunks(ns, 4096, kChunks, [&](size_t u0, size_t u1, int k) {
+    parallel_chunks(np, 2048, kChunks, [&](size_t q0, size_t q1, int k) {
+      const size_t u0 = 2 * q0, u1 = 2 * q1;
       size_t at = at0[k];
       uint64_t w = w0[k], cur = 0, po = 0;
       uint32_t pl = 0;
@@ -1118,7 +1115,7 @@ int upload_plan(sf_plan* P, BuildScratch& S) {
   const uint64_t tb_words = P->tb_words, ops_words = P->ops_words;
   const uint64_t scratch_total = S.scratch_total, snap_words = S.snap_words;
   int rc;
-  if ((rc = P->d_bytes.ensure(std::max<uint64_t>(P->pool_bytes, 16)))) return rc;
+  if (!P->bytes_from && (rc = P->d_bytes.ensure(std::max<uint64_t>(P->pool_bytes, 16)))) return rc;
   if ((rc = P->d_pool.ensure(P->pool_words * 4))) return rc;
   const size_t nseq = P->seq_boff.size();
   if ((rc = P->d_seq.ensure(nseq * 20 + 64))) return rc;
@@ -1259,26 +1256,36 @@ int plan_build(sf_plan* P) {
   return SF_OK;
 }
 
-// Launches one execute.  With `evs`, everything runs in order on `s` with an event recorded
-// after each stage (pack, each bucket, walk + compaction) for per-stage timing.
-int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = nullptr) {
+// The device copy of the plan's byte pool: its own, or the one it borrows.
+const uint8_t* plan_dev_bytes(const sf_plan* P) {
+  return P->bytes_from ? P->bytes_from : P->d_bytes.as<uint8_t>();
+}
+
+// With `evs`, records an event on `s` (per-stage timing).
+int mark_stage(std::vector<cudaEvent_t>* evs, cudaStream_t s) {
+  if (!evs) return SF_OK;
+  cudaEvent_t e;
+  CK(cudaEventCreate(&e));
+  evs->push_back(e);
+  CK(cudaEventRecord(e, s));
+  return SF_OK;
+}
+
+// The first part of an execute: the pack on `s`, then the buckets, fanned out over the
+// auxiliary streams so that their tails overlap (bucket u on stream (u + soff) mod kAux;
+// also a single bucket with `fan_one`).  `used` collects the auxiliary streams launched on.
+// With `evs`, everything runs in order on `s` with an event after each stage.
+int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs, int soff,
+                        bool fan_one, bool* used) {
   sf_context* ctx = P->ctx;
   uint64_t launches = 0;
-  auto mark = [&]() -> int {
-    if (!evs) return SF_OK;
-    cudaEvent_t e;
-    CK(cudaEventCreate(&e));
-    evs->push_back(e);
-    CK(cudaEventRecord(e, s));
-    return SF_OK;
-  };
   int mrc;
-  if ((mrc = mark())) return mrc;
+  if ((mrc = mark_stage(evs, s))) return mrc;
   CK(cudaMemsetAsync(P->d_counters.p, 0, P->buckets.size() * 4 + 4, s));
   {
     const size_t nseq = P->seq_boff.size();
     sfk::PackLaunch pl;
-    pl.bytes = P->d_bytes.as<uint8_t>();
+    pl.bytes = plan_dev_bytes(P);
     pl.byte_off = P->d_seq.as<uint64_t>();
     pl.word_off = reinterpret_cast<const uint64_t*>(P->d_seq.as<uint8_t>() + nseq * 8);
     pl.len = reinterpret_cast<const uint32_t*>(P->d_seq.as<uint8_t>() + nseq * 16);
@@ -1288,19 +1295,19 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
     CK(sfk::launch_pack(pl, s));
     launches += nseq ? 1 : 0;
   }
-  if ((mrc = mark())) return mrc;
-  // Buckets fan out over the auxiliary streams so that their tails overlap.
+  if ((mrc = mark_stage(evs, s))) return mrc;
   const int nb = (int)P->buckets.size();
-  const bool fan = !evs && nb > 1;
-  bool used[sf_context::kAux] = {};
+  const bool fan = !evs && (nb > 1 || (fan_one && nb == 1));
+  bool mine[sf_context::kAux] = {};
   if (fan) CK(cudaEventRecord(ctx->fork, s));
   for (int q = 0; q < nb; ++q) {
     const Bucket& b = P->buckets[q];
     cudaStream_t bs = s;
     if (fan) {
-      bs = ctx->aux[b.stream];
-      if (!used[b.stream]) CK(cudaStreamWaitEvent(bs, ctx->fork, 0));
-      used[b.stream] = true;
+      const int si = (b.stream + soff) % sf_context::kAux;
+      bs = ctx->aux[si];
+      if (!mine[si]) CK(cudaStreamWaitEvent(bs, ctx->fork, 0));
+      mine[si] = used[si] = true;
     }
     uint32_t* counter = P->d_counters.as<uint32_t>() + q;
     const uint32_t* order = P->d_order.as<uint32_t>() + b.first;
@@ -1322,7 +1329,7 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
       al.njobs = b.count;
       al.counter = counter;
       al.pool = P->d_pool.as<uint32_t>();
-      al.bytes = P->d_bytes.as<uint8_t>();
+      al.bytes = plan_dev_bytes(P);
       al.out = P->d_res.as<DRes>();
       al.tb = P->d_tb.as<uint32_t>();
       al.scratch = P->d_scratch.as<int32_t>() + b.scratch_off;
@@ -1344,25 +1351,42 @@ int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = null
         CK(sfk::launch_affine(b.c, b.wide, b.tb, b.kind == PK_LOCAL, al, b.grid, b.block, bs));
     }
     launches++;
-    if ((mrc = mark())) return mrc;
+    if ((mrc = mark_stage(evs, s))) return mrc;
   }
-  if (fan) {
-    for (int i = 0; i < sf_context::kAux; ++i) {
-      if (!used[i]) continue;
-      CK(cudaEventRecord(ctx->join[i], ctx->aux[i]));
-      CK(cudaStreamWaitEvent(s, ctx->join[i], 0));
-    }
+  P->launches = launches;
+  return SF_OK;
+}
+
+// The auxiliary streams in `used` joined back into `s`.
+int join_aux(sf_context* ctx, cudaStream_t s, const bool* used) {
+  for (int i = 0; i < sf_context::kAux; ++i) {
+    if (!used[i]) continue;
+    CK(cudaEventRecord(ctx->join[i], ctx->aux[i]));
+    CK(cudaStreamWaitEvent(s, ctx->join[i], 0));
   }
+  return SF_OK;
+}
+
+// The last part of an execute, after its buckets: the passes walked their own paths
+// (sf_walk.cuh); the CIGARs are compacted.
+int plan_launch_compact(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs) {
   if (P->n_walk) {
-    // The passes walked their own paths (sf_walk.cuh); compact the CIGARs.
     CK(sfk::launch_compact(P->d_tres.as<TRes>(), P->d_tjobs.as<TJob>(), P->d_wlist.as<uint32_t>(),
                            P->n_walk, P->d_offs.as<uint64_t>(), P->d_ops.as<uint32_t>(),
                            P->d_opsc.as<uint32_t>(), P->d_total.as<uint64_t>(), s));
-    launches += 2;
+    P->launches += 2;
   }
-  if ((mrc = mark())) return mrc;
-  P->launches = launches;
-  return SF_OK;
+  return mark_stage(evs, s);
+}
+
+// Launches one execute on `s`.  With `evs`, everything runs in order on `s` with an event
+// recorded after each stage (pack, each bucket, walk + compaction) for per-stage timing.
+int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = nullptr) {
+  bool used[sf_context::kAux] = {};
+  int rc;
+  if ((rc = plan_launch_buckets(P, s, evs, 0, false, used))) return rc;
+  if ((rc = join_aux(P->ctx, s, used))) return rc;
+  return plan_launch_compact(P, s, evs);
 }
 
 int plan_execute(sf_plan* P, bool use_graph) {
@@ -1732,7 +1756,7 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
 // Fills `results` from the fetched per-pass records; with `copy_ops`, also copies the CIGARs
 // fetched into h_ops to `ops` (sf_plan_download copies them straight from the device).
 int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
-                 uint64_t total, bool copy_ops) {
+                 uint64_t total, bool copy_ops, uint64_t ops_base) {
   if (total && (!ops || ops_cap < total)) {
     return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
   }
@@ -1793,6 +1817,7 @@ int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_c
     }
     ops_of[k + 1] = n_ops;
   });
+  ops_of[0] = ops_base;
   for (int k = 0; k < kT; ++k) ops_of[k + 1] += ops_of[k];
   parallel_chunks(np, 2048, kT, [&](size_t q0, size_t q1, int k) {
     uint64_t acc = ops_of[k];
@@ -2575,6 +2600,124 @@ int sf_sorted_batch(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes,
   return SF_OK;
 }
 
+namespace {
+
+// Jobs per segment of a batch: a batch of fewer than twice this runs as one plan.
+constexpr uint64_t kSegJobs = 4096;
+
+// Whether a batch's jobs are even enough to run in segments: no job's estimated work above
+// 8x the mean.  A long pass in a late segment starts only when the earlier segments' blocks
+// have left the device, so it would end after the rest; one plan starts it first.  Work is
+// band cells for affine jobs and matrix cells / 24 for Myers (its cells cost about 1/24 of
+// an affine cell).
+bool batch_even(const sf_job_t* jobs, uint64_t count) {
+  constexpr int kT = 8;
+  double sum[kT] = {}, mx[kT] = {};
+  parallel_chunks(count, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    double s = 0, x = 0;
+    for (size_t q = q0; q < q1; ++q) {
+      const sf_job_t& j = jobs[q];
+      const double m = j.m, n = j.n;
+      double w;
+      if (j.kind == SF_JOB_MYERS) {
+        w = m * n / 24.0;
+      } else {
+        const double band = j.band == SF_NOLIMIT ? n + 1 : 2.0 * (double)j.band + 1;
+        w = m * std::min(n + 1, band);
+      }
+      s += w;
+      x = std::max(x, w);
+    }
+    sum[k] = s;
+    mx[k] = x;
+  });
+  double s = 0, x = 0;
+  for (int k = 0; k < kT; ++k) {
+    s += sum[k];
+    x = std::max(x, mx[k]);
+  }
+  return count > 0 && x <= 8.0 * (s / (double)count);
+}
+
+// A large batch in segments of consecutive jobs, each its own plan: the host converts and
+// builds segment k + 1 while the device runs segment k, and each segment's buckets start on
+// the auxiliary streams after the last segment's, so that one segment's tail overlaps the
+// next one's start.  The pool goes to the device once, into the first segment's plan, which
+// the later segments read.  Errors are found in job order as in one plan: segment k's jobs
+// are checked before segment k + 1's are converted.
+int batch_run_segments(sf_context* ctx, int nseg, const uint8_t* pool, uint64_t pool_bytes,
+                       const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
+                       uint32_t n_scores, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
+                       uint64_t* ops_used) {
+  sf_plan* seg[sf_context::kSegs];
+  seg[0] = ctx->cache.get();
+  for (int k = 1; k < nseg; ++k) {
+    auto& sp = ctx->segs[k - 1];
+    if (!sp) {
+      sp.reset(new sf_plan);
+      sp->ctx = ctx;
+    }
+    seg[k] = sp.get();
+  }
+  uint64_t lo[sf_context::kSegs + 1];
+  for (int k = 0; k <= nseg; ++k) lo[k] = count * (uint64_t)k / (uint64_t)nseg;
+  CK(cudaSetDevice(ctx->dev));
+  sf_plan* P0 = seg[0];
+  P0->bytes_from = nullptr;
+  P0->pool_bytes = pool_bytes;
+  int rc;
+  if ((rc = P0->d_bytes.ensure(std::max<uint64_t>(pool_bytes, 16)))) return rc;
+  if ((rc = plan_upload_from(P0, pool))) return rc;
+  bool used[sf_context::kAux] = {};
+  int soff = 0;
+  for (int k = 0; k < nseg; ++k) {
+    sf_plan* P = seg[k];
+    rc = jobs_to_passes(jobs + lo[k], lo[k + 1] - lo[k], scores, n_scores, pool_bytes, P->passes,
+                        ctx->store);
+    if (rc == SF_OK) {
+      P->pool_bytes = pool_bytes;
+      P->bytes_from = k ? P0->d_bytes.as<uint8_t>() : nullptr;
+      rc = plan_build(P);
+    }
+    if (rc == SF_OK) rc = plan_launch_buckets(P, ctx->s, nullptr, soff, true, used);
+    if (rc != SF_OK) {
+      // Earlier segments' kernels end before the call returns: the next call reuses their
+      // buffers.  The first error stays the reported one.
+      const std::string msg = last_error();
+      (void)join_aux(ctx, ctx->s, used);
+      (void)cudaStreamSynchronize(ctx->s);
+      return fail(rc, msg);
+    }
+    soff = (soff + (int)std::max<size_t>(P->buckets.size(), 1)) % sf_context::kAux;
+  }
+  if ((rc = join_aux(ctx, ctx->s, used))) return rc;
+  for (int k = 0; k < nseg; ++k)
+    if ((rc = plan_launch_compact(seg[k], ctx->s, nullptr))) return rc;
+  // Results: each segment's records, its CIGARs after the earlier segments' ones.
+  uint64_t base[sf_context::kSegs + 1] = {};
+  for (int k = 0; k < nseg; ++k) {
+    if ((rc = plan_fetch(seg[k]))) return rc;
+    base[k + 1] = base[k] + (seg[k]->n_walk ? *seg[k]->h_total.as<uint64_t>() : 0);
+  }
+  const uint64_t total = base[nseg];
+  if (ops_used) *ops_used = total;
+  if (total && (!ops || ops_cap < total)) return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
+  for (int k = 0; k < nseg; ++k) {
+    const uint64_t n = base[k + 1] - base[k];
+    if (n) CK(cudaMemcpyAsync(ops + base[k], seg[k]->d_opsc.p, n * 4, cudaMemcpyDeviceToHost, ctx->s));
+  }
+  if (total) CK(cudaStreamSynchronize(ctx->s));
+  for (int k = 0; k < nseg; ++k) {
+    const uint64_t n = base[k + 1] - base[k];
+    if ((rc = plan_results(seg[k], results + lo[k], n ? ops + base[k] : nullptr, n, n, false,
+                           base[k])))
+      return rc;
+  }
+  return SF_OK;
+}
+
+}  // namespace
+
 int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, const sf_job_t* jobs,
                  uint64_t count, const sf_affine_t* scores, uint32_t n_scores,
                  sf_result_t* results, uint32_t* ops, uint64_t ops_cap, uint64_t* ops_used) {
@@ -2585,7 +2728,12 @@ int sf_batch_run(sf_context* ctx, const uint8_t* pool, uint64_t pool_bytes, cons
     ctx->cache.reset(new sf_plan);
     ctx->cache->ctx = ctx;
   }
+  const int nseg = (int)std::min<uint64_t>(count / kSegJobs, sf_context::kSegs);
+  if (nseg >= 2 && batch_segments_on() && batch_even(jobs, count))
+    return batch_run_segments(ctx, nseg, pool, pool_bytes, jobs, count, scores, n_scores, results,
+                              ops, ops_cap, ops_used);
   sf_plan* P = ctx->cache.get();
+  P->bytes_from = nullptr;
   int rc = jobs_to_passes(jobs, count, scores, n_scores, pool_bytes, P->passes, ctx->store);
   if (rc) return rc;
   P->pool_bytes = pool_bytes;

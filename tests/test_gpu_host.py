@@ -68,3 +68,75 @@ def test_pool_out_of_job_order(env):
     out = B.run(ctx, pool.build(), jobs)
     for q in range(0, count, 37):
         assert int(out.results[q]["distance"]) == O.myers_distance(p, texts[q], R.INFIX), q
+
+
+@pytest.mark.parametrize("count", [10001, 16411])
+def test_neighbours_share_sequences_across_chunks(env, count):
+    """Job q aligns sequence q to sequence q + 1, so each job's text is the next job's
+    pattern: one stored copy per sequence, also where a chunk of jobs starts."""
+    B, ctx = env
+    rng = np.random.default_rng(count + 1)
+    pool = B.PoolBuilder()
+    seqs, offs = [], []
+    for _ in range(count + 1):
+        s = rng.integers(0, 4, int(rng.integers(1, 70))).astype(np.uint8)
+        offs.append(pool.add(s))
+        seqs.append(s)
+    jobs = B.new_jobs(count)
+    for q in range(count):
+        j = jobs[q]
+        j["p_off"], j["t_off"] = offs[q], offs[q + 1]
+        j["m"], j["n"] = seqs[q].size, seqs[q + 1].size
+        j["kind"] = B.JOB_MYERS if q % 2 else B.JOB_AFFINE
+        j["mode"] = R.GLOBAL
+        j["band"] = 80
+    out = B.run(ctx, pool.build(), jobs)
+    for q in range(0, count, 7):
+        r = out.results[q]
+        if q % 2:
+            assert int(r["distance"]) == O.myers_distance(seqs[q], seqs[q + 1], R.GLOBAL), q
+        else:
+            assert int(r["score"]) == O.affine(seqs[q], seqs[q + 1], R.GLOBAL, R.ONT, 80), q
+
+
+@pytest.mark.parametrize("count", [8192, 13001, 40000])
+def test_segmented_batch_equals_one_plan(env, count, monkeypatch):
+    """A large batch runs in segments (each its own plan, the next built while the last
+    runs): every result field and every CIGAR op equals the one-plan run's, CIGAR offsets
+    follow job order across segments, and the CIGARs score what the results say."""
+    B, ctx = env
+    rng = np.random.default_rng(count + 2)
+    pool = B.PoolBuilder()
+    jobs = B.new_jobs(count)
+    pairs = []
+    for q in range(count):
+        t = rng.integers(0, 4, int(rng.integers(100, 260))).astype(np.uint8)
+        p = t[rng.random(t.size) > 0.04]  # deletions, then substitutions
+        sub = rng.random(p.size) < 0.05
+        p[sub] = (p[sub] + 1) & 3
+        j = jobs[q]
+        j["p_off"], j["t_off"] = pool.add(p), pool.add(t)
+        j["m"], j["n"] = p.size, t.size
+        kind = q % 4
+        j["kind"] = B.JOB_MYERS if kind == 0 else B.JOB_AFFINE
+        j["mode"] = (R.GLOBAL, R.PREFIX, R.INFIX)[q % 3] if kind == 0 else (R.GLOBAL, R.PREFIX)[q % 2]
+        j["want_cigar"] = kind in (1, 2)
+        j["band"] = int(rng.integers(20, 100))  # even work: the batch runs in segments
+        pairs.append((p, t))
+    built = pool.build()
+    monkeypatch.setenv("SF_BATCH_SEGMENTS", "0")
+    one = B.run(ctx, built, jobs)
+    monkeypatch.setenv("SF_BATCH_SEGMENTS", "1")
+    seg = B.run(ctx, built, jobs)
+    for name in one.results.dtype.names:
+        assert np.array_equal(one.results[name], seg.results[name]), name
+    assert np.array_equal(one.ops, seg.ops)
+    cig = np.nonzero(jobs["want_cigar"])[0]
+    offs = seg.results["cigar_off"][cig]
+    assert np.all(np.diff(offs.astype(np.int64)) >= 0)
+    for q in cig[:: max(1, len(cig) // 60)]:
+        r = seg.results[q]
+        assert r["status"] == 0, q
+        p, t = pairs[q]
+        score, used, _ = O.cigar_score(p, t, seg.cigar(q), int(r["text_start"]), R.ONT)
+        assert (score, used) == (int(r["score"]), int(r["pattern_end"])), q
