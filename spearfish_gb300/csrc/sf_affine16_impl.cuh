@@ -37,6 +37,11 @@ constexpr uint32_t kOne2 = 0x00010001u;
 constexpr uint32_t kNeg2 = kNeg16 * kOne2;
 constexpr uint32_t kGt2 = 0x7fff7fffu;
 constexpr int kRebaseRows = 64;
+// Score-only classes of up to this many words a lane run their steady rows in groups of C/2
+// with the text selectors rotated by renaming (one copy of the row per group position).
+// Measured on GB300: score-only 20,000 x 2 kb, band 128, 1,750 -> 1,880 GCUPS; with
+// traceback the longer rows lost 4-14% (classes 8-16) and stay on register moves.
+constexpr int kRenameC2 = 8;
 
 __device__ __forceinline__ uint32_t pk2(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
 
@@ -283,9 +288,14 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
   int32_t Wc = 0, ks = 0;
   uint32_t ms = 0;
   bool sent = false;
-  auto row = [&](int32_t i, auto modetag) -> bool {
+  // ROT < 0: the row shifts the text selectors down one register (sel[k] = column k).
+  // ROT = r >= 0 (steady rows in groups of C2, the group's row r): the selectors rotate by
+  // renaming instead, register (k + r) mod C2 holding column k before the row's shift, and
+  // the shift overwrites the register of the column that leaves.
+  auto row = [&](int32_t i, auto modetag, auto rottag) -> bool {
     // MODE 0: lo = 0; 1: lo moves right by one; 2: as 1, with i + above <= n.
     constexpr int MODE = decltype(modetag)::value;
+    constexpr int ROT = decltype(rottag)::value;
     constexpr bool D1 = MODE >= 1, ST = MODE == 2;
     // align.rs:2462-2468; rows past n + below (empty) never get here.
     const int32_t lo = D1 ? i - g.below : 0, hi = ST ? i + g.above : min(i + g.above, n);
@@ -295,16 +305,20 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
     pw >>= 2;
     const uint32_t ta = (mpm & 0xffu) << pb, tbl = (mpm >> 8) << pb;
     if (D1 && i > 1) {
-      const uint32_t s0 = sel[0];
+      constexpr int R0 = ROT < 0 ? 0 : ROT;
+      const uint32_t s0 = sel[R0];
       uint32_t nx = __shfl_down_sync(FULL, s0, 1);
       // The column entering lane 31 (32-bit positions: texts are shorter than 2^31).
       const uint32_t fcol = (uint32_t)(lo + 32 * C - 1);
       const uint32_t fw = __ldg(a.pool + x.J.t_word + (fcol >> 4));
       const uint32_t far = sel_byte((fw >> (2u * (fcol & 15u))) & 3u);
       if (lane == 31) nx = far;
+      if constexpr (ROT < 0) {
 #pragma unroll
-      for (int k = 0; k + 1 < C2; ++k) sel[k] = sel[k + 1];
-      sel[C2 - 1] = __byte_perm(s0, nx, 0x2241);  // (old word 0 high column, next lane's low)
+        for (int k = 0; k + 1 < C2; ++k) sel[k] = sel[k + 1];
+      }
+      // (old word 0 high column, next lane's low)
+      sel[ROT < 0 ? C2 - 1 : R0] = __byte_perm(s0, nx, 0x2241);
     }
 
     // Pass 1: F, H' and the lane's horizontal-gap chain.  F = max(Hup - go, Fup - ext): the
@@ -319,7 +333,9 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
       const uint32_t ho = hu * one - go2;
       const uint32_t fo = fu * one - ext2;
       const uint32_t fj = __vmaxu2(ho, fo);
-      const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);  // diagonal + s + mis
+      // This row's column k, after its shift.
+      constexpr int sk = (D1 && ROT >= 0) ? (k + ROT + 1) % C2 : k;
+      const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[sk]);  // diagonal + s + mis
       const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
       if constexpr (TB)
         acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), xx - dgp + kGtDg);
@@ -476,8 +492,10 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
   const int64_t lastB = (int64_t)n + g.below;  // the last row whose band is not empty
   const int32_t endB = (int64_t)m < lastB ? m : (int32_t)lastB;
   const int32_t endS = min(endB, n - g.above);  // the last row with i + above <= n
+  using Shift = std::integral_constant<int, -1>;
+  using Steady = std::integral_constant<int, 2>;
   for (int32_t i = first; i <= endA && !stopped; ++i)
-    stopped = row(i, std::integral_constant<int, 0>{});
+    stopped = row(i, std::integral_constant<int, 0>{}, Shift{});
   int32_t i1 = max(endA + 1, first);
   if (i1 <= endS) {
     Wc = g.below + g.above + 1;
@@ -486,10 +504,22 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
     ks = c < C2 ? c : c - C2;
     ms = lane == Ls ? (c < C2 ? 0xffffu : 0xffff0000u) : 0u;
     Wm = -1;
-    for (; i1 <= endS && !stopped; ++i1) stopped = row(i1, std::integral_constant<int, 2>{});
+    if constexpr (C2 <= kRenameC2 && !TB) {
+      // Whole groups of C2 rows rotate the selectors by renaming (back in place after each
+      // group); the rows left over shift them.  Row 1 shifts nothing: it runs first.
+      if (i1 == 1 && !stopped) stopped = row(i1++, Steady{}, Shift{});
+      while (i1 + C2 - 1 <= endS && !stopped) {
+        sf_unroll<C2>([&](auto rt) {
+          if (stopped) return;
+          stopped = row(i1, Steady{}, std::integral_constant<int, decltype(rt)::value>{});
+          ++i1;
+        });
+      }
+    }
+    for (; i1 <= endS && !stopped; ++i1) stopped = row(i1, Steady{}, Shift{});
   }
   for (int32_t i = i1; i <= endB && !stopped; ++i)
-    stopped = row(i, std::integral_constant<int, 1>{});
+    stopped = row(i, std::integral_constant<int, 1>{}, Shift{});
   if (!stopped && endB < m) {
     // Row endB + 1 lies past the text: the pass ends there with no score (align.rs:2543-2553).
     r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)(endB + 1),

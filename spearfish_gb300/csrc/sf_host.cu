@@ -346,11 +346,17 @@ class HostPool {
 // on the host pool's threads, when every chunk gets at least min_per_thread items (else one
 // chunk on the calling thread).  The same (n, min_per_thread, max_threads) always gives the
 // same chunks; a chunk the pool cannot take runs on the calling thread.
+// How many chunks parallel_chunks(n, min_per_thread, max_threads, ...) makes.
+size_t chunks_for(size_t n, size_t min_per_thread, int max_threads) {
+  const size_t t = std::min<size_t>({HostPool::get().workers() + 1, (size_t)max_threads,
+                                     min_per_thread ? n / min_per_thread : 1});
+  return std::max<size_t>(t, 1);
+}
+
 template <class F>
 void parallel_chunks(size_t n, size_t min_per_thread, int max_threads, F&& f) {
   HostPool& pool = HostPool::get();
-  size_t t = std::min<size_t>({pool.workers() + 1, (size_t)max_threads,
-                               min_per_thread ? n / min_per_thread : 1});
+  const size_t t = chunks_for(n, min_per_thread, max_threads);
   if (t <= 1) {
     f(size_t(0), n, 0);
     return;
@@ -912,7 +918,8 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
              (k.tb & ~1) == 0 && k.lanes >= 0 && k.lanes < 64;
     };
     auto& bits = S.code_bits;
-    bits.assign((size_t)kT * kWords, 0);
+    const size_t nt = chunks_for(ni, 4096, kT);  // the chunks below: each its own bit set
+    bits.assign(nt * kWords, 0);
     bool packed[kT];
     std::fill(packed, packed + kT, true);
     parallel_chunks(ni, 4096, kT, [&](size_t q0, size_t q1, int k) {
@@ -933,7 +940,7 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
       std::vector<uint32_t> below(kWords + 1, 0);
       for (uint32_t w = 0; w < kWords; ++w) {
         uint64_t x = 0;
-        for (int k = 0; k < kT; ++k) x |= bits[(size_t)k * kWords + w];
+        for (size_t k = 0; k < nt; ++k) x |= bits[k * kWords + w];
         bits[w] = x;
         below[w + 1] = below[w] + (uint32_t)__builtin_popcountll(x);
         for (; x; x &= x - 1) {
@@ -1010,7 +1017,7 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
     return (uint32_t)(16 * (e - 3) + ((w >> (e - 4)) & 15));
   };
   constexpr uint32_t kBins = 16 * 61 + 16;
-  constexpr size_t kBig = 16384;
+  constexpr size_t kBig = 4096;
   auto& tmp = S.byb_tmp;
   std::vector<uint64_t> bin_at((size_t)kT * kBins);
   for (size_t u = 0; u < nb; ++u) {
@@ -1019,27 +1026,36 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
     const auto* src = byb.data() + b.first;
     const size_t n = b.count;
     std::fill(bin_at.begin(), bin_at.end(), 0);
-    parallel_chunks(n, 4096, kT, [&](size_t e0, size_t e1, int k) {
+    parallel_chunks(n, 2048, kT, [&](size_t e0, size_t e1, int k) {
       uint64_t* c = bin_at.data() + (size_t)k * kBins;
       for (size_t e = e0; e < e1; ++e) c[kBins - 1 - wbin(src[e].first)]++;
     });
     uint64_t acc = 0;
-    for (uint32_t v = 0; v < kBins; ++v)
+    uint32_t bins_used = 0;
+    for (uint32_t v = 0; v < kBins; ++v) {
+      const uint64_t a0 = acc;
       for (int k = 0; k < kT; ++k) {
         const uint64_t c = bin_at[(size_t)k * kBins + v];
         bin_at[(size_t)k * kBins + v] = acc;
         acc += c;
       }
-    tmp.resize(n);
-    parallel_chunks(n, 4096, kT, [&](size_t e0, size_t e1, int k) {
-      uint64_t* a = bin_at.data() + (size_t)k * kBins;
-      for (size_t e = e0; e < e1; ++e) tmp[a[kBins - 1 - wbin(src[e].first)]++] = src[e];
-    });
+      bins_used += acc > a0;
+    }
+    // One bin (work alike): job order is the order.
+    const std::pair<uint64_t, uint32_t>* sorted = src;
+    if (bins_used > 1) {
+      tmp.resize(n);
+      parallel_chunks(n, 2048, kT, [&](size_t e0, size_t e1, int k) {
+        uint64_t* a = bin_at.data() + (size_t)k * kBins;
+        for (size_t e = e0; e < e1; ++e) tmp[a[kBins - 1 - wbin(src[e].first)]++] = src[e];
+      });
+      sorted = tmp.data();
+    }
     uint64_t lat[kT] = {};
-    parallel_chunks(n, 4096, kT, [&](size_t e0, size_t e1, int k) {
+    parallel_chunks(n, 2048, kT, [&](size_t e0, size_t e1, int k) {
       uint64_t l = 0;
       for (size_t e = e0; e < e1; ++e) {
-        const BucketItem& it = items[tmp[e].second].second;
+        const BucketItem& it = items[sorted[e].second].second;
         order[b.first + e] = it.slot;
         l = std::max(l, it.lat);
       }
@@ -1047,7 +1063,7 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
     });
     b.lat = *std::max_element(lat, lat + kT);
   }
-  parallel_chunks(nb, ni >= kBig ? 1 : nb + 1, kT, [&](size_t u0, size_t u1, int) {
+  parallel_chunks(nb, ni >= 16384 ? 1 : nb + 1, kT, [&](size_t u0, size_t u1, int) {
     std::vector<uint32_t> bin_n(kBins + 1);
     std::vector<std::pair<uint64_t, uint32_t>> part;
     for (size_t u = u0; u < u1; ++u) {
