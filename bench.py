@@ -178,7 +178,7 @@ AFFINE16H_C = (8, 10, 12, 14, 16, 18, 20, 24)  # the same with 16 lanes a pass
 
 
 def fits16(j, w, sc, B) -> bool:
-    """sf_host.cu fits16: Global/Prefix banded passes whose values fit 16-bit fields."""
+    """sf_plan.cu fits16: Global/Prefix banded passes whose values fit 16-bit fields."""
     if j["kind"] == B.JOB_LOCAL or j["mode"] == 0 or int(j["band"]) == 2 ** 64 - 1:
         return False
     mat, mis, opn, ext = sc
@@ -192,7 +192,7 @@ MYERS_B = (1, 2, 3, 4, 6, 8, 12, 16)
 
 
 def job_classes(jobs, B, scores=((2, 4, 4, 2),)):
-    """The kernel class each job runs in, by the library's bucketing rule (sf_host.cu)."""
+    """The kernel class each job runs in, by the library's bucketing rule (sf_plan.cu)."""
     out = []
     for j in jobs:
         m, n = int(j["m"]), int(j["n"])

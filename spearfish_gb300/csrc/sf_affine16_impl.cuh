@@ -12,7 +12,7 @@
 // (`rebase`), so all reachable values stay within a window of 16384 below and a few hundred
 // above field 0x8000; NEG is field 0x4000, below every reachable value by more than any
 // single step can add.  The host admits a pass only when its widest row, its scores and this
-// bound fit (sf_host.cu `fits16`); everything else runs on the 32-bit kernel.
+// bound fit (sf_plan.cu `fits16`); everything else runs on the 32-bit kernel.
 //
 // Layout.  A field holds value - offset (offset = -0x8000 at row 0), unsigned, so the DPX
 // u16x2 maxima order fields as values, and a - b + 0x7fff7fff has bit 15 (31) set exactly

@@ -1,5 +1,5 @@
-// Internal engine of libsf_align: buffers, passes, plans and contexts shared by the C ABI
-// (sf_host.cu) and the serving loop (sf_server.cu).  Not part of the public ABI.
+// Internal engine of libsf_align: buffers, passes, plans and contexts shared by the plans
+// (sf_plan.cu), the C ABI (sf_host.cu) and the serving loop (sf_server.cu).  Not part of the public ABI.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -207,9 +207,9 @@ struct sf_plan {
   const sf_store* store = nullptr;
   // Class overrides for this plan only (the autotuner's trial plans); else the context's.
   const sfe::TuneTable* tune_override = nullptr;
-  // Host-side build arrays kept between builds (sf_host.cu).
+  // Host-side build arrays kept between builds (sf_plan.cu).
   std::unique_ptr<sfe::BuildScratch> scratch;
-  // Out of line (sf_host.cu): deleting an owned context needs sf_context complete, and the
+  // Out of line (sf_plan.cu): deleting an owned context needs sf_context complete, and the
   // build arrays their type.
   sf_plan();
   ~sf_plan();
@@ -278,6 +278,32 @@ int plan_fetch_ops(sf_plan* P, uint64_t& total);
 // `ops_base` is added to every cigar_off (the ops of earlier segments before `ops`).
 int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
                  uint64_t total, bool copy_ops = true, uint64_t ops_base = 0);
+// Argument checks shared by the entry points: a mode of SF_INFIX/PREFIX/GLOBAL, and scores
+// with non-negative gap costs.
+bool ok_mode(int mode);
+bool ok_sc(const sf_affine_t* sc);
+// Kernel classes (sf_plan.cu).
+bool allow16();
+int default_lanes16();
+void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, PassKind& kind,
+                     int& c, bool& wide, int& lanes, int lanes16 = 32);
+int choose_myers_class(uint32_t m, int& b, int& lanes);
+DJob make_djob(const Pass& p, uint32_t& flags);
+// Whether large sf_batch_run batches may run in segments (SF_BATCH_SEGMENTS).
+bool batch_segments_on();
+// The plan's pinned staging: stage_done marks the end of the copies issued out of it so
+// far; stage_wait waits for that before it is written again.
+int stage_wait(sf_plan* P);
+int stage_done(sf_plan* P);
+// One execute in parts: the pack and the buckets (bucket u on auxiliary stream
+// (u + soff) mod kAux, also a single bucket with fan_one; `used` collects the streams),
+// the auxiliary streams joined back into `s`, then the CIGAR compaction.  plan_launch runs
+// all three; with `evs`, everything runs in order on `s` with an event after each stage.
+int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs, int soff,
+                        bool fan_one, bool* used);
+int join_aux(sf_context* ctx, cudaStream_t s, const bool* used);
+int plan_launch_compact(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs);
+int plan_launch(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs = nullptr);
 // Device bytes a plan of these passes needs (upper bound, before building it).
 uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_bytes);
 // Device bytes the plan's buffers hold now.
