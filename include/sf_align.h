@@ -264,7 +264,10 @@ int sf_plan_create(sf_context *ctx, const sf_job_t *jobs, uint64_t count,
                    const sf_affine_t *scores, uint32_t n_scores,
                    uint64_t pool_bytes, sf_plan **out);
 void sf_plan_destroy(sf_plan *plan);
-/* Host pool -> device (pinned staging, async on the plan's stream). */
+/* Host pool -> device, copied on the plan's stream straight from `pool`.  From
+ * pinned memory the copy is asynchronous: keep the pool unchanged until the
+ * plan's stream has passed it (sf_plan_sync, sf_plan_download).  From pageable
+ * memory the call returns once the bytes are staged. */
 int sf_plan_upload(sf_plan *plan, const uint8_t *pool);
 /* Run every job on the resident inputs (asynchronous). */
 int sf_plan_execute(sf_plan *plan);
