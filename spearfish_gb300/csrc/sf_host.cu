@@ -950,6 +950,26 @@ namespace {
 // Jobs per segment of a batch: a batch of fewer than twice this runs as one plan.
 constexpr uint64_t kSegJobs = 4096;
 
+// The end of the furthest pool byte the jobs read (patterns, and texts in the pool), at most
+// pool_bytes.
+uint64_t pool_reach(const sf_job_t* jobs, uint64_t count, uint64_t pool_bytes) {
+  constexpr int kT = 8;
+  uint64_t mx[kT] = {};
+  auto end = [&](uint64_t off, uint64_t len) {
+    return off >= pool_bytes || len > pool_bytes - off ? pool_bytes : off + len;
+  };
+  parallel_chunks(count, 4096, kT, [&](size_t q0, size_t q1, int k) {
+    uint64_t x = 0;
+    for (size_t q = q0; q < q1; ++q) {
+      const sf_job_t& j = jobs[q];
+      x = std::max(x, end(j.p_off, j.m));
+      if (j.text_src == SF_TEXT_POOL) x = std::max(x, end(j.t_off, j.n));
+    }
+    mx[k] = x;
+  });
+  return *std::max_element(mx, mx + kT);
+}
+
 // Whether a batch's jobs are even enough to run in segments: no job's estimated work above
 // 8x the mean.  A long pass in a late segment starts only when the earlier segments' blocks
 // have left the device, so it would end after the rest; one plan starts it first.  Work is
@@ -1007,16 +1027,25 @@ int batch_run_segments(sf_context* ctx, int nseg, const uint8_t* pool, uint64_t 
   uint64_t lo[sf_context::kSegs + 1];
   for (int k = 0; k <= nseg; ++k) lo[k] = count * (uint64_t)k / (uint64_t)nseg;
   CK(cudaSetDevice(ctx->dev));
+  if (pool_bytes && !pool) return fail(SF_ERR_INVALID, "null pool");
   sf_plan* P0 = seg[0];
   P0->bytes_from = nullptr;
   P0->pool_bytes = pool_bytes;
   int rc;
   if ((rc = P0->d_bytes.ensure(std::max<uint64_t>(pool_bytes, 16)))) return rc;
-  if ((rc = plan_upload_from(P0, pool))) return rc;
   bool used[sf_context::kAux] = {};
   int soff = 0;
+  uint64_t up = 0;  // pool bytes copied so far
   for (int k = 0; k < nseg; ++k) {
     sf_plan* P = seg[k];
+    // The pool goes up in prefixes: before a segment, the bytes up to the furthest one its
+    // jobs read (in a pool laid out in job order, about a segment's share).
+    const uint64_t reach = pool_reach(jobs + lo[k], lo[k + 1] - lo[k], pool_bytes);
+    if (reach > up) {
+      CK(cudaMemcpyAsync(P0->d_bytes.as<uint8_t>() + up, pool + up, reach - up,
+                         cudaMemcpyHostToDevice, ctx->s));
+      up = reach;
+    }
     rc = jobs_to_passes(jobs + lo[k], lo[k + 1] - lo[k], scores, n_scores, pool_bytes, P->passes,
                         ctx->store);
     if (rc == SF_OK) {
