@@ -270,7 +270,6 @@ namespace sfe {
 uint64_t seq_words(uint64_t len) { return (len + 1 + 15) / 16; }
 
 
-// Builds descriptors, buckets and device buffers for `passes` (pool not yet uploaded).
 // h_stage holds data for asynchronous copies on the context's stream: stage_done marks the
 // end of the copies issued so far, and stage_wait waits for it before the staging is written
 // or reallocated again.
@@ -1311,9 +1310,6 @@ int plan_upload_from(sf_plan* P, const uint8_t* pool) {
   CK(cudaSetDevice(ctx->dev));
   if (!P->pool_bytes) return SF_OK;
   if (!pool) return fail(SF_ERR_INVALID, "null pool");
-  cudaPointerAttributes at{};
-  cudaError_t e = cudaPointerGetAttributes(&at, pool);
-  if (e != cudaSuccess) (void)cudaGetLastError();
   CK(cudaMemcpyAsync(P->d_bytes.p, pool, P->pool_bytes, cudaMemcpyHostToDevice, ctx->s));
   return SF_OK;
 }
