@@ -425,7 +425,7 @@ def main():
                     help="c5: texts as windows of a device-resident transcript store (1) or in "
                          "each request's pool (0)")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload's pairs")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--plain-pairs", type=int, default=200)
