@@ -240,9 +240,13 @@ struct sf_context {
   cudaStream_t aux[kAux] = {};
   cudaEvent_t fork = nullptr, join[kAux] = {};
   std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
-  // sf_batch_run's later segments of a large batch (the first is `cache`).
+  // sf_batch_run's later segments of a large batch (the first is `cache`), and the stream
+  // each segment's tail (CIGAR compaction, copies back) runs on while later segments run,
+  // with an event per segment at its tail's end.
   static constexpr int kSegs = 4;
   std::unique_ptr<sf_plan> segs[kSegs - 1];
+  cudaStream_t tail = nullptr;
+  cudaEvent_t seg_done[kSegs] = {};
   sfe::TuneTable tune;             // autotuner choices, applied to every later plan
   sf_store* store = nullptr;       // transcript store for SF_TEXT_STORE texts
   ~sf_context() {
@@ -255,6 +259,9 @@ struct sf_context {
       if (aux[i]) cudaStreamDestroy(aux[i]);
       if (join[i]) cudaEventDestroy(join[i]);
     }
+    for (auto& e : seg_done)
+      if (e) cudaEventDestroy(e);
+    if (tail) cudaStreamDestroy(tail);
     if (fork) cudaEventDestroy(fork);
     if (s) cudaStreamDestroy(s);
     cudaSetDevice(prev);
@@ -273,6 +280,8 @@ int plan_build(sf_plan* P);
 int plan_upload_from(sf_plan* P, const uint8_t* pool);
 int plan_execute(sf_plan* P, bool use_graph);
 int plan_fetch(sf_plan* P);
+// The copies of plan_fetch, queued on `s` without waiting.
+int plan_fetch_async(sf_plan* P, cudaStream_t s);
 int plan_fetch_ops(sf_plan* P, uint64_t& total);
 // Converts a fetched plan's results to sf_result_t (and copies compacted ops).
 // `ops_base` is added to every cigar_off (the ops of earlier segments before `ops`).

@@ -1007,9 +1007,11 @@ bool batch_even(const sf_job_t* jobs, uint64_t count) {
 // A large batch in segments of consecutive jobs, each its own plan: the host converts and
 // builds segment k + 1 while the device runs segment k, and each segment's buckets start on
 // the auxiliary streams after the last segment's, so that one segment's tail overlaps the
-// next one's start.  The pool goes to the device once, into the first segment's plan, which
-// the later segments read.  Errors are found in job order as in one plan: segment k's jobs
-// are checked before segment k + 1's are converted.
+// next one's start.  Each segment's CIGAR compaction and copies back run on the context's
+// tail stream as soon as its buckets end, and the host converts its results while later
+// segments run.  The pool goes to the device once, into the first segment's plan, which the
+// later segments read.  Errors are found in job order as in one plan: segment k's jobs are
+// checked before segment k + 1's are converted.
 int batch_run_segments(sf_context* ctx, int nseg, const uint8_t* pool, uint64_t pool_bytes,
                        const sf_job_t* jobs, uint64_t count, const sf_affine_t* scores,
                        uint32_t n_scores, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
@@ -1053,40 +1055,59 @@ int batch_run_segments(sf_context* ctx, int nseg, const uint8_t* pool, uint64_t 
       P->bytes_from = k ? P0->d_bytes.as<uint8_t>() : nullptr;
       rc = plan_build(P);
     }
-    if (rc == SF_OK) rc = plan_launch_buckets(P, ctx->s, nullptr, soff, true, used);
+    bool mine[sf_context::kAux] = {};
+    if (rc == SF_OK) rc = plan_launch_buckets(P, ctx->s, nullptr, soff, true, mine);
+    for (int i = 0; i < sf_context::kAux; ++i) used[i] = used[i] || mine[i];
+    // The segment's tail on the tail stream, while later segments run: its buckets joined,
+    // its CIGARs compacted, its records copied back.
+    if (rc == SF_OK) rc = join_aux(ctx, ctx->tail, mine);
+    if (rc == SF_OK) rc = plan_launch_compact(P, ctx->tail, nullptr);
+    if (rc == SF_OK) rc = plan_fetch_async(P, ctx->tail);
+    if (rc == SF_OK && cudaEventRecord(ctx->seg_done[k], ctx->tail) != cudaSuccess)
+      rc = fail(SF_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     if (rc != SF_OK) {
-      // Earlier segments' kernels end before the call returns: the next call reuses their
-      // buffers.  The first error stays the reported one.
+      // Earlier segments' kernels and tails end before the call returns: the next call
+      // reuses their buffers.  The first error stays the reported one.
       const std::string msg = last_error();
       (void)join_aux(ctx, ctx->s, used);
       (void)cudaStreamSynchronize(ctx->s);
+      (void)cudaStreamSynchronize(ctx->tail);
       return fail(rc, msg);
     }
     soff = (soff + (int)std::max<size_t>(P->buckets.size(), 1)) % sf_context::kAux;
   }
-  if ((rc = join_aux(ctx, ctx->s, used))) return rc;
-  for (int k = 0; k < nseg; ++k)
-    if ((rc = plan_launch_compact(seg[k], ctx->s, nullptr))) return rc;
-  // Results: each segment's records, its CIGARs after the earlier segments' ones.
+  // Results, segment by segment as their tails end: the records converted while later
+  // segments run, the CIGARs copied to the caller after the earlier segments' ones.
   uint64_t base[sf_context::kSegs + 1] = {};
-  for (int k = 0; k < nseg; ++k) {
-    if ((rc = plan_fetch(seg[k]))) return rc;
-    base[k + 1] = base[k] + (seg[k]->n_walk ? *seg[k]->h_total.as<uint64_t>() : 0);
+  bool fits = true;
+  for (int k = 0; k < nseg && rc == SF_OK; ++k) {
+    if (cudaEventSynchronize(ctx->seg_done[k]) != cudaSuccess) {
+      rc = fail(SF_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    const uint64_t n = seg[k]->n_walk ? *seg[k]->h_total.as<uint64_t>() : 0;
+    base[k + 1] = base[k] + n;
+    if (!fits || (n && (!ops || base[k + 1] > ops_cap))) {
+      fits = false;  // the remaining totals are still counted for ops_used
+      continue;
+    }
+    // On the main stream (idle by now): the tail stream still holds later segments' tails.
+    if (n && cudaMemcpyAsync(ops + base[k], seg[k]->d_opsc.p, n * 4, cudaMemcpyDeviceToHost,
+                             ctx->s) != cudaSuccess) {
+      rc = fail(SF_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    rc = plan_results(seg[k], results + lo[k], n ? ops + base[k] : nullptr, n, n, false, base[k]);
   }
-  const uint64_t total = base[nseg];
-  if (ops_used) *ops_used = total;
-  if (total && (!ops || ops_cap < total)) return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
-  for (int k = 0; k < nseg; ++k) {
-    const uint64_t n = base[k + 1] - base[k];
-    if (n) CK(cudaMemcpyAsync(ops + base[k], seg[k]->d_opsc.p, n * 4, cudaMemcpyDeviceToHost, ctx->s));
-  }
-  if (total) CK(cudaStreamSynchronize(ctx->s));
-  for (int k = 0; k < nseg; ++k) {
-    const uint64_t n = base[k + 1] - base[k];
-    if ((rc = plan_results(seg[k], results + lo[k], n ? ops + base[k] : nullptr, n, n, false,
-                           base[k])))
-      return rc;
-  }
+  // Every copy into the caller's buffers, and all of the call's device work, has ended when
+  // the call returns.
+  cudaError_t e = cudaStreamSynchronize(ctx->tail);
+  const cudaError_t e2 = cudaStreamSynchronize(ctx->s);
+  if (e == cudaSuccess) e = e2;
+  if (rc != SF_OK) return rc;
+  if (e != cudaSuccess) return fail(SF_ERR_CUDA, cudaGetErrorString(e));
+  if (ops_used) *ops_used = base[nseg];
+  if (!fits) return fail(SF_ERR_CAPACITY, "ops buffer smaller than the CIGARs");
   return SF_OK;
 }
 

@@ -51,6 +51,8 @@ int make_context(int device, sf_context** out) {
     CK(cudaEventCreateWithFlags(&c->join[i], cudaEventDisableTiming));
   }
   CK(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&c->tail, cudaStreamNonBlocking));
+  for (auto& ev : c->seg_done) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   *out = c.release();
   return SF_OK;
 }
@@ -1315,20 +1317,25 @@ int plan_upload_from(sf_plan* P, const uint8_t* pool) {
 }
 
 // Results -> host pinned buffers (and compacted ops), then the caller's arrays.
-int plan_fetch(sf_plan* P) {
-  sf_context* ctx = P->ctx;
+int plan_fetch_async(sf_plan* P, cudaStream_t s) {
   int rc;
   if ((rc = P->h_res.ensure(P->n_aff * sizeof(DRes) + 64))) return rc;
   if ((rc = P->h_mout.ensure(P->n_my * 4 + 64))) return rc;
   if ((rc = P->h_tres.ensure(P->n_aff * sizeof(TRes) + 64))) return rc;
-  if (P->n_aff) CK(cudaMemcpyAsync(P->h_res.p, P->d_res.p, P->n_aff * sizeof(DRes), cudaMemcpyDeviceToHost, ctx->s));
-  if (P->n_my) CK(cudaMemcpyAsync(P->h_mout.p, P->d_mout.p, P->n_my * 4, cudaMemcpyDeviceToHost, ctx->s));
+  if (P->n_aff) CK(cudaMemcpyAsync(P->h_res.p, P->d_res.p, P->n_aff * sizeof(DRes), cudaMemcpyDeviceToHost, s));
+  if (P->n_my) CK(cudaMemcpyAsync(P->h_mout.p, P->d_mout.p, P->n_my * 4, cudaMemcpyDeviceToHost, s));
   if (P->n_walk) {
-    CK(cudaMemcpyAsync(P->h_tres.p, P->d_tres.p, P->n_aff * sizeof(TRes), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(P->h_tres.p, P->d_tres.p, P->n_aff * sizeof(TRes), cudaMemcpyDeviceToHost, s));
     if ((rc = P->h_total.ensure(64))) return rc;
-    CK(cudaMemcpyAsync(P->h_total.p, P->d_total.p, 8, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(P->h_total.p, P->d_total.p, 8, cudaMemcpyDeviceToHost, s));
   }
-  CK(cudaStreamSynchronize(ctx->s));
+  return SF_OK;
+}
+
+int plan_fetch(sf_plan* P) {
+  int rc;
+  if ((rc = plan_fetch_async(P, P->ctx->s))) return rc;
+  CK(cudaStreamSynchronize(P->ctx->s));
   return SF_OK;
 }
 
