@@ -1339,10 +1339,6 @@ int plan_fetch(sf_plan* P) {
   return SF_OK;
 }
 
-struct Fetched {
-  uint64_t ops_total = 0;
-};
-
 int plan_fetch_ops(sf_plan* P, uint64_t& total) {
   sf_context* ctx = P->ctx;
   total = 0;
