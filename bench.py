@@ -278,7 +278,7 @@ def cpu_baseline(cfg, pairs_list, seconds: float, threads: int, variant: str = "
             "sample": f"{done} of {len(w)} pairs ({total_cells / 1e9:.2f} Gcells, "
                       f"{total_t:.1f} s wall on {threads} threads, score only: the reference "
                       f"computes no traceback)",
-            "arch": platform.machine()}
+            "wall_s": total_t, "arch": platform.machine()}
 
 
 def kslack_caps(w, threads: int) -> np.ndarray:
@@ -303,11 +303,15 @@ def run_reference(args, ws, rank):
         if s >= args.warmup:
             per_step.append(r)
     v = statistics.mean(r["value"] for r in per_step)
+    # A step is one bounded sample of the workload (about ref_seconds of work).
+    ms = 1e3 * statistics.mean(r["wall_s"] for r in per_step)
     line = {"metric": "alignment GCUPS", "value": v, "unit": "GCUPS", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": workload_name(args), "parallelism": "host threads"},
+            "config": {"workload": workload_name(args), "parallelism": "host threads",
+                       "step": "a bounded sample of the workload's pairs"},
             "cpu_baseline": {"value": v, "unit": "GCUPS", "cores": threads, "kind": "port",
                              "sample": per_step[-1]["sample"], "level": per_step[-1]["level"]},
             "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0,

@@ -41,6 +41,22 @@ def test_reference_arm_variants(args, workload):
     assert d["e2e"]["h2d_bytes_per_step"] == 0
 
 
+def test_reference_line_carries_the_contract_keys():
+    """The keys a bench line must carry, with their types, on the reference arm's line."""
+    r = run("--config", "c2", "--scale", "0.002")
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    for k, t in (("metric", str), ("value", float), ("unit", str), ("n_gpus", int),
+                 ("steps", int), ("warmup", int), ("higher_is_better", bool),
+                 ("scaling", str), ("dtype", str), ("data", str), ("config", dict),
+                 ("e2e", dict), ("cpu_baseline", dict)):
+        assert isinstance(d.get(k), t), (k, d.get(k))
+    assert "vs_baseline" in d and "ms_per_step" in d
+    assert d["impl"] == "reference" and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["unit"] == d["unit"] and d["e2e"]["value"] == d["value"]
+
+
 def test_variant_of_another_config_is_refused():
     r = run("--config", "c3", "--variant", "window", "--scale", "0.002")
     assert r.returncode != 0
