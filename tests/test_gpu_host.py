@@ -140,3 +140,38 @@ def test_segmented_batch_equals_one_plan(env, count, monkeypatch):
         p, t = pairs[q]
         score, used, _ = O.cigar_score(p, t, seg.cigar(q), int(r["text_start"]), R.ONT)
         assert (score, used) == (int(r["score"]), int(r["pattern_end"])), q
+
+
+@pytest.mark.parametrize("count", [300, 9000])
+def test_ops_buffer_too_small(env, count):
+    """An ops buffer smaller than the CIGARs: SF_ERR_CAPACITY with ops_used set to what the
+    CIGARs need (one plan, and a batch in segments), and the context stays usable."""
+    import ctypes as C
+    from spearfish_gb300 import _abi
+    B, ctx = env
+    rng = np.random.default_rng(count + 3)
+    pool = B.PoolBuilder()
+    jobs = B.new_jobs(count)
+    for q in range(count):
+        t = rng.integers(0, 4, int(rng.integers(150, 200))).astype(np.uint8)
+        p = t[rng.random(t.size) > 0.03]
+        j = jobs[q]
+        j["p_off"], j["t_off"], j["m"], j["n"] = pool.add(p), pool.add(t), p.size, t.size
+        j["kind"], j["mode"], j["want_cigar"], j["band"] = B.JOB_AFFINE, R.GLOBAL, 1, 40
+    built = pool.build()
+    good = B.run(ctx, built, jobs)
+    need = good.ops.size
+    assert need > 0
+    lib = _abi.load()
+    sc = (_abi.Affine * 1)(_abi.Affine(2, 4, 4, 2))
+    res = np.zeros(count, dtype=B.RESULT_DTYPE)
+    ops = np.zeros(need, dtype=np.uint32)
+    used = C.c_uint64()
+    rc = lib.sf_batch_run(ctx.handle, built.ctypes.data_as(C.POINTER(C.c_uint8)), built.size,
+                          jobs.ctypes.data_as(C.POINTER(_abi.JobT)), count, sc, 1,
+                          res.ctypes.data_as(C.POINTER(_abi.ResultT)),
+                          ops.ctypes.data_as(C.POINTER(C.c_uint32)), need // 2, C.byref(used))
+    assert rc == -6  # SF_ERR_CAPACITY (include/sf_align.h)
+    assert used.value == need
+    again = B.run(ctx, built, jobs)
+    assert np.array_equal(again.results, good.results) and np.array_equal(again.ops, good.ops)
