@@ -283,6 +283,11 @@ void *sf_plan_stream(sf_plan *plan);
 uint64_t sf_plan_launches(const sf_plan *plan);
 /* Description of the plan's buckets as a static-lifetime JSON string. */
 const char *sf_plan_describe(sf_plan *plan);
+/* Each job's bucket: buckets[q] = the index, in sf_plan_describe's list, of
+ * the bucket whose kernel runs job q (SF_NONE for a job that a row-sharing
+ * chain runs).  `count` >= the plan's jobs.  No reference counterpart: the
+ * reference has no buckets; this lets a caller attribute work per kernel. */
+int sf_plan_job_buckets(const sf_plan *plan, uint32_t *buckets, uint64_t count);
 
 /* Runs one execute in order on the plan's stream with CUDA events between
  * its stages -- pack, each bucket (in sf_plan_describe's order; a bucket
@@ -503,7 +508,12 @@ int sf_server_query(sf_server *srv, sf_server_stats *out);
  * SF_NOALLOC_MAX_LEN bases each (SF_ERR_TOO_LONG beyond).  Calls whose work
  * overlaps on one GPU race on the array: order them (one stream).  The first
  * call on a device looks the array up with that device current; make it
- * before any stream capture. */
+ * before any stream capture.  The address is kept for the process: after a
+ * cudaDeviceReset of that device the library must be loaded afresh before
+ * this entry point is called again.  A score-only pass has no failure outcome
+ * on the device (an unreachable end is NEG, as `affine` returns), so every
+ * error is reported by the return code.  Its cells and rows are not added to
+ * sf_dp_work's counters: the call returns before the pass has run. */
 #define SF_NOALLOC_SCRATCH (1u << 19)
 #define SF_NOALLOC_MAX_LEN 16384u
 int sf_affine_noalloc(const uint8_t *d_pattern, uint64_t m,

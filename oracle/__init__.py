@@ -118,8 +118,12 @@ def lib():
         L.or_run_pairs.restype = C.c_uint64
         L.or_run_pairs.argtypes = [C.c_int, C.c_int, _u8p, _u64p, _u64p, _u8p, _u64p, _u64p,
                                    C.c_uint64, C.c_int, C.c_uint32, C.POINTER(C.c_uint32),
-                                   C.POINTER(Affine), C.c_uint64, C.POINTER(ExtendOpts),
-                                   _i64p]
+                                   C.POINTER(Affine), C.c_uint64, _u64p, C.POINTER(ExtendOpts),
+                                   _i64p, _u64p]
+        L.or_check_cigars.restype = C.c_uint64
+        L.or_check_cigars.argtypes = [C.c_int, _u8p, _u64p, _u64p, _u8p, _u64p, _u64p,
+                                      C.c_uint64, _u32p, _u64p, _u32p, _u64p, _u64p, _i32p,
+                                      C.POINTER(Affine), _i32p]
         _lib = L
     return _lib
 
@@ -307,24 +311,51 @@ def set_level(level: int) -> int:
 
 def run_pairs(kind: int, threads: int, pseq, poff, plen, tseq, toff, tlen, mode: int,
               k: int = 0xFFFFFFFF, sc=ONT, band=None, kv=None,
-              extend: Optional[tuple] = None) -> tuple[np.ndarray, int]:
-    """All pairs on `threads` host threads; returns (per-pair result, cells).  kind 0:
-    Myers (cap k, or per pair kv); 1: affine; 2: extend window, extend = (pad, pad_div,
-    xdrop, end_bonus)."""
+              extend: Optional[tuple] = None, bands=None,
+              per_pair_cells: bool = False):
+    """All pairs on `threads` host threads; returns (per-pair result, cells), or (per-pair
+    result, per-pair cells) with per_pair_cells.  kind 0: Myers (cap k, or per pair kv);
+    1: affine; 2: extend window, extend = (pad, pad_div, xdrop, end_bonus).  bands: a band
+    per pair (instead of `band`)."""
     count = len(plen)
     out = np.zeros(count, dtype=np.int64)
     arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
             ((pseq, np.uint8), (poff, np.uint64), (plen, np.uint64), (tseq, np.uint8),
              (toff, np.uint64), (tlen, np.uint64))]
     kva = None if kv is None else np.ascontiguousarray(kv, dtype=np.uint32)
+    bva = None if bands is None else np.ascontiguousarray(bands, dtype=np.uint64)
+    cpp = np.zeros(count, dtype=np.uint64) if per_pair_cells else None
     ext = ExtendOpts(*extend) if extend is not None else None
     cells = lib().or_run_pairs(kind, threads, _p(arrs[0]), _p(arrs[1], _u64p),
                                _p(arrs[2], _u64p), _p(arrs[3]), _p(arrs[4], _u64p),
                                _p(arrs[5], _u64p), count, mode, k,
                                None if kva is None else _p(kva, C.POINTER(C.c_uint32)),
                                C.byref(_sc(sc)), _band(band),
-                               None if ext is None else C.byref(ext), _p(out, _i64p))
+                               None if bva is None else _p(bva, _u64p),
+                               None if ext is None else C.byref(ext), _p(out, _i64p),
+                               None if cpp is None else _p(cpp, _u64p))
+    if per_pair_cells:
+        return out, cpp
     return out, int(cells)
+
+
+def check_cigars(threads: int, pseq, poff, plen, tseq, toff, tlen, ops, cig_off, n_ops,
+                 text_start, text_end, score, sc=ONT) -> np.ndarray:
+    """Re-scores every pair's CIGAR (or_check_cigars); returns a code per pair: 0 the path
+    consumes the pattern, ends at text_end and scores `score`; 1 another score; 2 the
+    pattern not consumed exactly; 3 another text end; 4 an op outside the sequences."""
+    count = len(plen)
+    code = np.zeros(count, dtype=np.int32)
+    a = [np.ascontiguousarray(x, dtype=dt) for x, dt in
+         ((pseq, np.uint8), (poff, np.uint64), (plen, np.uint64), (tseq, np.uint8),
+          (toff, np.uint64), (tlen, np.uint64), (ops, np.uint32), (cig_off, np.uint64),
+          (n_ops, np.uint32), (text_start, np.uint64), (text_end, np.uint64),
+          (score, np.int32))]
+    lib().or_check_cigars(threads, _p(a[0]), _p(a[1], _u64p), _p(a[2], _u64p), _p(a[3]),
+                          _p(a[4], _u64p), _p(a[5], _u64p), count, _p(a[6], _u32p),
+                          _p(a[7], _u64p), _p(a[8], _u32p), _p(a[9], _u64p), _p(a[10], _u64p),
+                          _p(a[11], _i32p), C.byref(_sc(sc)), _p(code, _i32p))
+    return code
 
 
 def host_threads() -> int:

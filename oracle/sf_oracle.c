@@ -1097,9 +1097,11 @@ typedef struct {
     const uint8_t *pseq, *tseq;
     const uint64_t *poff, *plen, *toff, *tlen;
     uint64_t count, band;
+    const uint64_t *bv;
     const or_affine_t *sc;
     or_extend_opts_t ext;
     int64_t *out;
+    uint64_t *cells_out;
     _Atomic uint64_t next;
     _Atomic uint64_t cells;
     int level;
@@ -1113,47 +1115,113 @@ static void *pair_worker(void *arg) {
         if (q >= j->count) break;
         const uint8_t *p = j->pseq + j->poff[q], *t = j->tseq + j->toff[q];
         uint64_t m = j->plen[q], n = j->tlen[q];
+        const uint64_t band = j->bv ? j->bv[q] : j->band;
+        uint64_t c;
         if (j->kind == 0) {
             j->out[q] = or_myers_distance(p, m, t, n, j->mode, j->kv ? j->kv[q] : j->k);
-            cells += m * n;
+            c = m * n;
         } else if (j->kind == 2) {
             /* align.rs:957-982 `affine_extend_window` with the mapper's window
              * x + pad + x / pad_div (map/src/lib.rs:2101). */
             const uint64_t w = m + j->ext.pad + (j->ext.pad_div ? m / j->ext.pad_div : 0);
             or_dp_t d;
-            run_core(p, m, t, n, OR_PREFIX, j->sc, j->band, umax(w, n), 1, j->ext.xdrop, 1,
+            run_core(p, m, t, n, OR_PREFIX, j->sc, band, umax(w, n), 1, j->ext.xdrop, 1,
                      OR_NOLIMIT, &d, NULL, j->level);
             const int32_t whole = sat_add32(d.score, j->ext.end_bonus);
             j->out[q] = d.clip_best >= whole ? d.clip_best : whole;
-            cells += d.cells;
+            c = d.cells;
         } else {
             or_dp_t d;
-            run_core(p, m, t, n, j->mode, j->sc, j->band, n, 0, 0, 0, OR_NOLIMIT, &d, NULL,
+            run_core(p, m, t, n, j->mode, j->sc, band, n, 0, 0, 0, OR_NOLIMIT, &d, NULL,
                      j->level);
             j->out[q] = d.score;
-            cells += d.cells;
+            c = d.cells;
         }
+        if (j->cells_out) j->cells_out[q] = c;
+        cells += c;
     }
     atomic_fetch_add(&j->cells, cells);
     return NULL;
+}
+
+static void run_workers(void *(*fn)(void *), void *arg, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 512) threads = 512;
+    pthread_t tid[512];
+    for (int i = 1; i < threads; i++) pthread_create(&tid[i], NULL, fn, arg);
+    fn(arg);
+    for (int i = 1; i < threads; i++) pthread_join(tid[i], NULL);
 }
 
 uint64_t or_run_pairs(int kind, int threads, const uint8_t *pseq, const uint64_t *poff,
                       const uint64_t *plen, const uint8_t *tseq, const uint64_t *toff,
                       const uint64_t *tlen, uint64_t count, int mode, uint32_t k,
                       const uint32_t *kv, const or_affine_t *sc, uint64_t band,
-                      const or_extend_opts_t *ext, int64_t *out) {
+                      const uint64_t *bv, const or_extend_opts_t *ext, int64_t *out,
+                      uint64_t *cells_out) {
     pair_job job = {.kind = kind, .mode = mode, .k = k, .kv = kv, .pseq = pseq, .tseq = tseq,
                     .poff = poff, .plen = plen, .toff = toff, .tlen = tlen, .count = count,
-                    .band = band, .sc = sc, .out = out, .level = atomic_load(&g_level)};
+                    .band = band, .bv = bv, .sc = sc, .out = out, .cells_out = cells_out,
+                    .level = atomic_load(&g_level)};
     if (ext) job.ext = *ext;
     atomic_store(&job.next, 0);
     atomic_store(&job.cells, 0);
-    if (threads < 1) threads = 1;
-    if (threads > 512) threads = 512;
-    pthread_t tid[512];
-    for (int i = 1; i < threads; i++) pthread_create(&tid[i], NULL, pair_worker, &job);
-    pair_worker(&job);
-    for (int i = 1; i < threads; i++) pthread_join(tid[i], NULL);
+    run_workers(pair_worker, &job, threads);
     return atomic_load(&job.cells);
+}
+
+/* ======================================================================
+ * CIGAR checks of a whole batch (test infrastructure): each pair's ops
+ * re-scored with or_cigar_score, on `threads` workers.
+ * ====================================================================== */
+
+typedef struct {
+    const uint8_t *pseq, *tseq;
+    const uint64_t *poff, *plen, *toff, *tlen;
+    const uint32_t *ops;
+    const uint64_t *cig_off, *text_start, *text_end;
+    const uint32_t *n_ops;
+    const int32_t *score;
+    const or_affine_t *sc;
+    uint64_t count;
+    int32_t *code;
+    _Atomic uint64_t next, bad;
+} cigar_job;
+
+static void *cigar_worker(void *arg) {
+    cigar_job *j = arg;
+    uint64_t bad = 0;
+    for (;;) {
+        uint64_t q = atomic_fetch_add(&j->next, 1);
+        if (q >= j->count) break;
+        uint64_t pu = 0, te = 0;
+        const int64_t s = or_cigar_score(j->pseq + j->poff[q], j->plen[q], j->tseq + j->toff[q],
+                                         j->tlen[q], j->ops + j->cig_off[q], j->n_ops[q],
+                                         j->text_start[q], j->sc, &pu, &te);
+        int32_t c = 0;
+        if (s == INT64_MIN) c = 4;
+        else if (pu != j->plen[q]) c = 2;
+        else if (te != j->text_end[q]) c = 3;
+        else if (s != (int64_t)j->score[q]) c = 1;
+        j->code[q] = c;
+        bad += c != 0;
+    }
+    atomic_fetch_add(&j->bad, bad);
+    return NULL;
+}
+
+uint64_t or_check_cigars(int threads, const uint8_t *pseq, const uint64_t *poff,
+                         const uint64_t *plen, const uint8_t *tseq, const uint64_t *toff,
+                         const uint64_t *tlen, uint64_t count, const uint32_t *ops,
+                         const uint64_t *cig_off, const uint32_t *n_ops,
+                         const uint64_t *text_start, const uint64_t *text_end,
+                         const int32_t *score, const or_affine_t *sc, int32_t *code) {
+    cigar_job job = {.pseq = pseq, .tseq = tseq, .poff = poff, .plen = plen, .toff = toff,
+                     .tlen = tlen, .ops = ops, .cig_off = cig_off, .text_start = text_start,
+                     .text_end = text_end, .n_ops = n_ops, .score = score, .sc = sc,
+                     .count = count, .code = code};
+    atomic_store(&job.next, 0);
+    atomic_store(&job.bad, 0);
+    run_workers(cigar_worker, &job, threads);
+    return atomic_load(&job.bad);
 }

@@ -161,14 +161,32 @@ typedef struct {
 /* Jobs: Myers distance per pair (kind 0; cap kv[q] when kv is not NULL, else
  * k), `affine` per pair (kind 1) or `affine_extend_window` per pair (kind 2,
  * whole score).  Sequences are byte codes; pair q is p[poff[q]..+plen[q]] vs
- * t[toff[q]..+tlen[q]].  out: int64 per pair.  Returns the summed DP_WORK
- * cells (affine) or m*n cells (Myers). */
+ * t[toff[q]..+tlen[q]]; its band is bv[q] when bv is not NULL, else band.
+ * out: int64 per pair; cells_out (may be NULL): each pair's cells.  Returns
+ * the summed DP_WORK cells (affine) or m*n cells (Myers). */
 uint64_t or_run_pairs(int kind, int threads, const uint8_t *pseq,
                       const uint64_t *poff, const uint64_t *plen,
                       const uint8_t *tseq, const uint64_t *toff,
                       const uint64_t *tlen, uint64_t count, int mode,
                       uint32_t k, const uint32_t *kv, const or_affine_t *sc,
-                      uint64_t band, const or_extend_opts_t *ext, int64_t *out);
+                      uint64_t band, const uint64_t *bv,
+                      const or_extend_opts_t *ext, int64_t *out,
+                      uint64_t *cells_out);
+
+/* CIGAR checks of a batch on `threads` workers: pair q's ops
+ * ops[cig_off[q]..+n_ops[q]] are re-scored from text base text_start[q]
+ * (or_cigar_score).  code[q]: 0 the path consumes the whole pattern, ends at
+ * text_end[q] and scores score[q]; 1 another score; 2 the pattern is not
+ * consumed exactly; 3 another text end; 4 an op leaves the sequences or is
+ * unknown.  Returns the number of pairs whose code is not 0. */
+uint64_t or_check_cigars(int threads, const uint8_t *pseq, const uint64_t *poff,
+                         const uint64_t *plen, const uint8_t *tseq,
+                         const uint64_t *toff, const uint64_t *tlen,
+                         uint64_t count, const uint32_t *ops,
+                         const uint64_t *cig_off, const uint32_t *n_ops,
+                         const uint64_t *text_start, const uint64_t *text_end,
+                         const int32_t *score, const or_affine_t *sc,
+                         int32_t *code);
 
 #ifdef __cplusplus
 }

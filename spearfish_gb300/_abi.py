@@ -173,6 +173,7 @@ SIGNATURES = {
     "sf_plan_stream": (_vp, [_vp]),
     "sf_plan_launches": (C.c_uint64, [_vp]),
     "sf_plan_describe": (C.c_char_p, [_vp]),
+    "sf_plan_job_buckets": (C.c_int, [_vp, _u32p, C.c_uint64]),
     "sf_plan_profile": (C.c_int, [_vp, C.POINTER(C.c_float), C.c_uint32, _u32p]),
     "sf_plan_tune": (C.c_int, [_vp, C.POINTER(C.c_uint8), C.c_uint32, C.c_char_p, C.c_uint64]),
     "sf_context_untune": (C.c_int, [_vp]),

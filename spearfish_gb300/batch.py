@@ -169,6 +169,15 @@ class Plan:
     def describe(self) -> str:
         return self._lib.sf_plan_describe(self.handle).decode()
 
+    def job_buckets(self) -> np.ndarray:
+        """Each job's bucket: its index in `describe()`'s bucket list (sf_plan_job_buckets;
+        0xFFFFFFFF for a job a row-sharing chain runs)."""
+        out = np.zeros(max(1, len(self.jobs)), dtype=np.uint32)
+        _abi.check(self._lib.sf_plan_job_buckets(self.handle,
+                                                 out.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                 len(self.jobs)))
+        return out[:len(self.jobs)]
+
     def tune(self, pool: np.ndarray, reps: int = 3) -> dict:
         """Autotunes the kernel classes of this plan's length buckets (sf_plan_tune): the
         choices stay in the context for later plans; the plan is rebuilt and its pool

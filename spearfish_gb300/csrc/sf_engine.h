@@ -277,6 +277,7 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
                    const sf_store* store = nullptr);
 // Descriptors, buckets and device buffers for P->passes (pool not yet uploaded).
 int plan_build(sf_plan* P);
+int plan_job_buckets(const sf_plan* P, uint32_t* out, uint64_t count);
 int plan_upload_from(sf_plan* P, const uint8_t* pool);
 int plan_execute(sf_plan* P, bool use_graph);
 int plan_fetch(sf_plan* P);

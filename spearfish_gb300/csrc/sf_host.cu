@@ -584,6 +584,11 @@ uint64_t sf_plan_launches(const sf_plan* plan) { return plan ? plan->launches : 
 
 const char* sf_plan_describe(sf_plan* plan) { return plan ? plan->desc.c_str() : ""; }
 
+int sf_plan_job_buckets(const sf_plan* plan, uint32_t* buckets, uint64_t count) {
+  if (!plan || (!buckets && count)) return fail(SF_ERR_INVALID, "bad argument");
+  return plan_job_buckets(plan, buckets, count);
+}
+
 int sf_plan_download(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_cap,
                      uint64_t* ops_used) {
   if (!P || (!results && !P->passes.empty())) return fail(SF_ERR_INVALID, "bad argument");

@@ -16,7 +16,10 @@
 // zero).  Calls whose work overlaps on one GPU -- on two streams, or from two threads --
 // race on the array; the caller must order them, e.g. by issuing them on one stream.  The
 // first call on a device looks the array's device address up (cudaGetSymbolAddress, with
-// that device current) and keeps it; make that first call before any stream capture.
+// that device current) and keeps it; make that first call before any stream capture.  A
+// cudaDeviceReset of that device invalidates the kept address (the module loads again,
+// maybe elsewhere): load the library afresh before calling this again.  The pass's cells are
+// not added to sf_dp_work's counters, since the call returns before the pass has run.
 #include <mutex>
 
 #include "../../include/sf_align.h"
@@ -73,6 +76,8 @@ __global__ void noalloc_prep(unsigned char* scr, DJob job, DParams params, uint3
     pool[w] = 0;
 }
 
+// The pass's score to the caller's buffer.  A score-only pass has no failure outcome on the
+// device (an unreachable end is NEG); launch errors come back as the return code.
 __global__ void noalloc_out(const unsigned char* scr, int32_t* out) {
   if (threadIdx.x == 0) *out = reinterpret_cast<const Header*>(scr)->res.score;
 }

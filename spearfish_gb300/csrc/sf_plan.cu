@@ -1146,6 +1146,30 @@ int plan_build(sf_plan* P) {
   return SF_OK;
 }
 
+// Each job's bucket, as its index in the plan's description (sf_plan_job_buckets);
+// SF_NONE for a pass that a row-sharing chain runs.
+int plan_job_buckets(const sf_plan* P, uint32_t* out, uint64_t count) {
+  const size_t np = P->passes.size();
+  if (count < np) return fail(SF_ERR_INVALID, "job_buckets: output shorter than the plan's jobs");
+  if (!P->scratch || P->scratch->per.size() != np) return fail(SF_ERR_INVALID, "job_buckets: plan not built");
+  const BuildScratch& S = *P->scratch;
+  std::vector<BucketKey> keys(P->buckets.size());
+  for (size_t u = 0; u < keys.size(); ++u) {
+    const Bucket& b = P->buckets[u];
+    keys[u] = BucketKey{(int)b.kind, b.c, b.wide ? 1 : 0, b.tb ? 1 : 0, b.lanes};
+  }
+  for (size_t q = 0; q < np; ++q) {
+    out[q] = SF_NONE;
+    if (!S.has_item[q]) continue;
+    for (size_t u = 0; u < keys.size(); ++u)
+      if (keys[u] == S.per[q].first) {
+        out[q] = (uint32_t)u;
+        break;
+      }
+  }
+  return SF_OK;
+}
+
 // The device copy of the plan's byte pool: its own, or the one it borrows.
 const uint8_t* plan_dev_bytes(const sf_plan* P) {
   return P->bytes_from ? P->bytes_from : P->d_bytes.as<uint8_t>();

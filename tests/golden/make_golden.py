@@ -162,7 +162,9 @@ def regressions(path: str) -> list[dict]:
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout (the spearfish source tree)>")
+    ref = sys.argv[1]
     reg = regressions(os.path.join(ref, "crates/map/proptest-regressions/align.txt"))
     doc = {"source": "COMBINE-lab/spearfish v0.3.2",
            "note": "KATs transcribed from the reference tests (cite = file:line); regressions "

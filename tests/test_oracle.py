@@ -224,3 +224,63 @@ def test_run_pairs_matches_single():
                                      for p, t, w in zip(ps, ts, win)]
     assert cells == sum(O.affine_dp(p, t, R.PREFIX, R.ONT, 16, geom=max(w, len(t)),
                                     clip=(50, True))["cells"] for p, t, w in zip(ps, ts, win))
+    # A band per pair, and each pair's cells.
+    bands = rng.integers(0, 40, len(ps)).astype(np.uint64)
+    out, cpp = O.run_pairs(1, 3, pc, po, pl, tc, to, tl, R.GLOBAL, sc=R.ONT, bands=bands,
+                           per_pair_cells=True)
+    assert [int(x) for x in out] == [O.affine(p, t, R.GLOBAL, R.ONT, int(b))
+                                     for p, t, b in zip(ps, ts, bands)]
+    assert [int(c) for c in cpp] == [O.affine_dp(p, t, R.GLOBAL, R.ONT, int(b))["cells"]
+                                     for p, t, b in zip(ps, ts, bands)]
+
+
+def test_check_cigars_batch():
+    """The batch CIGAR checker passes the oracle's own tracebacks and flags planted faults
+    (a changed op, a wrong score, a wrong text end, a truncated path)."""
+    rng = np.random.default_rng(23)
+    ps, ts, cig, offs, nops, starts, ends, scores = [], [], [], [], [], [], [], []
+    at = 0
+    for _ in range(30):
+        p, t = R.rand_pair(int(rng.integers(20, 400)), int(rng.integers(3, 15)),
+                           int(rng.integers(1, 2 ** 62)))
+        tb = O.traceback(p, t, O.TB_AFFINE, R.GLOBAL, R.ONT, 32)
+        assert tb["status"] == 0
+        ps.append(np.asarray(p, np.uint8))
+        ts.append(np.asarray(t, np.uint8))
+        cig.append(np.asarray(tb["cigar"], np.uint32))
+        offs.append(at)
+        at += len(tb["cigar"])
+        nops.append(len(tb["cigar"]))
+        starts.append(tb["text_start"])
+        ends.append(tb["end_j"])
+        scores.append(tb["score"])
+
+    def cat(xs):
+        lens = np.array([len(x) for x in xs], dtype=np.uint64)
+        o = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.uint64)
+        return np.concatenate(xs), o, lens
+
+    pc, po, pl = cat(ps)
+    tc, to, tl = cat(ts)
+    ops = np.concatenate(cig)
+    args = [np.array(offs, np.uint64), np.array(nops, np.uint32), np.array(starts, np.uint64),
+            np.array(ends, np.uint64), np.array(scores, np.int32)]
+    code = O.check_cigars(3, pc, po, pl, tc, to, tl, ops, *args, sc=R.ONT)
+    assert (code == 0).all()
+    bad_score = args[4].copy()
+    bad_score[3] += 1
+    assert list(np.flatnonzero(O.check_cigars(2, pc, po, pl, tc, to, tl, ops, *args[:4],
+                                              bad_score, sc=R.ONT))) == [3]
+    bad_end = args[3].copy()
+    bad_end[5] += 1
+    code = O.check_cigars(2, pc, po, pl, tc, to, tl, ops, *args[:3], bad_end, args[4],
+                          sc=R.ONT)
+    assert list(np.flatnonzero(code)) == [5] and code[5] == 3
+    short = args[1].copy()
+    short[7] -= 1
+    code = O.check_cigars(2, pc, po, pl, tc, to, tl, ops, args[0], short, *args[2:], sc=R.ONT)
+    assert code[7] != 0 and (np.delete(code, 7) == 0).all()
+    bad_op = ops.copy()
+    bad_op[offs[9]] = (bad_op[offs[9]] & ~np.uint32(15)) | 7  # an unknown op
+    code = O.check_cigars(2, pc, po, pl, tc, to, tl, bad_op, *args, sc=R.ONT)
+    assert code[9] == 4 and (np.delete(code, 9) == 0).all()
