@@ -464,8 +464,8 @@ def parity_check(cfg, pairs_list, res, ops, checked, threads) -> dict:
     return out
 
 
-def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, local, lib, cpu,
-                  plain_pairs, e2e_steps):
+def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, local, lib,
+                  with_cpu, plain_pairs, e2e_steps):
     """One workload as a batched plan: device-timed steps, per-kernel split, roofline of the
     top kernel, e2e through sf_batch_run, parity against the oracle, CPU baseline, plain."""
     import ctypes as C
@@ -653,7 +653,7 @@ def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, loca
     if rank == 0:
         import oracle as O
         threads = O.host_threads()
-        if cpu:
+        if with_cpu:
             cpu, checked = cpu_baseline(cfg, pairs_list, args.cpu_seconds, threads, variant, caps)
         else:  # the parity check alone, on a small sample
             _, checked = cpu_baseline(cfg, pairs_list, 0.5, threads, variant, caps)
@@ -688,7 +688,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c5"])
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="c5: stream length")
-    ap.add_argument("--sub-serve-seconds", type=float, default=12.0,
+    ap.add_argument("--sub-serve-seconds", type=float, default=30.0,
                     help="c3: length of the served stream in the `sub` object (0: none)")
     ap.add_argument("--sub", type=int, default=1,
                     help="c3: also measure config 2 and a served stream (1) or not (0)")

@@ -325,10 +325,13 @@ def serving_store_jobs(tx: Transcriptome, reads: list, B) -> tuple[np.ndarray, n
 
 
 def serving_stream(duration_s: float, reads_per_s: float = 2000.0, burst: float = 5.0,
-                   max_batch: int = 4096, seed: int = 5):
+                   max_batch: int = 4096, seed: int = 5, exact_mean: bool = True):
     """Arrivals of read batches: batch sizes log-uniform over 1..max_batch reads, batch
     arrivals Poisson, the rate switching between a base rate and `burst` times it (bursts of
     exponential length, mean 0.5 s, 10% of the time) so that the mean is `reads_per_s`.
+    A window of seconds holds few batches of very uneven size, so its own mean drifts far
+    from the stream's; with `exact_mean` the arrival times are scaled so that the window
+    offers exactly `reads_per_s` (reads / last arrival).
     Returns [(arrival seconds, reads in the batch)]."""
     rng = np.random.default_rng(seed)
     mean_batch = (max_batch - 1) / np.log(max_batch)
@@ -345,4 +348,7 @@ def serving_stream(duration_s: float, reads_per_s: float = 2000.0, burst: float 
         t += dt
         size = int(np.clip(np.round(np.exp(rng.uniform(0, np.log(max_batch)))), 1, max_batch))
         out.append((t, size))
+    if exact_mean and out:
+        f = sum(n for _, n in out) / reads_per_s / out[-1][0]
+        out = [(a * f, n) for a, n in out]
     return out
