@@ -73,6 +73,10 @@ def workload_name(cfg, variant="base", cigar=True) -> str:
 
 
 OPS_PER_CELL = {"affine_tb": 12, "affine": 10, "myers": 0.625}
+# sf_int_peak counts 3 int32 ops per chain step; ncu counts 2.094 instructions per step (an
+# IMAD on the FMA pipe and a fused add-max on the ALU pipe, the loop included), so its rate
+# in instructions is Tops x 2.094 / 3 (profiles/int_peak.md).
+INT_PEAK_INSTR_PER_STEP = 2.094
 
 
 def dist_env():
@@ -565,6 +569,8 @@ def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, loca
     achieved = top_cells * ops_cell / (top_ms * 1e-3) / 1e12
     peak = C.c_double()
     lib.sf_int_peak(local, C.byref(peak), None)
+    peak_instr = peak.value * INT_PEAK_INSTR_PER_STEP / 3
+    props = torch.cuda.get_device_properties(local)
     # HBM side of the same kernel: algorithmic bytes = its pairs' packed inputs (2 bits a base)
     # + 8 B of result each + half a byte of traceback bits per DP cell when it keeps them;
     # measured bytes = the ncu DRAM bytes per cell of this kernel, scaled to this launch.
@@ -588,11 +594,21 @@ def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, loca
             traffic = int(tr["bytes_per_cell"] * top_cells)
     except (OSError, ValueError):
         pass
+    issue = props.multi_processor_count * 4 * 32 * (clk.get("sm_mhz") or 0) * 1e6 / 1e12
     roofline = {"bound": "int32", "kernel": stages[1 + top], "achieved": achieved,
-                "peak": peak.value, "unit": "Tops/s",
-                "frac": achieved / peak.value if peak.value else None,
-                "peak_source": "measured on this GPU by sf_int_peak (int32 add-then-max mix); "
-                               "its instruction count is pinned in profiles/int_peak.md",
+                "peak": peak_instr, "unit": "T int32-instr/s",
+                "frac": achieved / peak_instr if peak_instr else None,
+                "achieved_note": "12 int32 ops per cell (10 without traceback), each one 32-bit "
+                                 "instruction in a scalar row; the kernel does two cells per "
+                                 "packed instruction where it can",
+                "peak_source": "sf_int_peak measured live on this GPU (add-then-max chains); "
+                               "restated in instructions: Tops x 2.094 / 3, the instructions "
+                               "ncu counts per 3-op step (profiles/int_peak.md)",
+                "peak_ops_tops": peak.value,
+                "frac_of_ops_peak": achieved / peak.value if peak.value else None,
+                "issue_ceiling": issue or None,
+                "issue_ceiling_note": "SMs x 4 schedulers x 32 lanes x median SM clock: one "
+                                      "instruction per scheduler per cycle",
                 "ops_per_cell": ops_cell, "cells_per_launch": top_cells,
                 "cells_source": "sf_plan_job_buckets (the library's bucketing) x DP_WORK cells",
                 "kernel_ms": top_ms, "share_of_kernel_time": top_ms / serial_ms if serial_ms else None,
