@@ -206,6 +206,12 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
   const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
   const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
   const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;  // gt2 against diagonal + mis
+  // Products with the opaque -1 issue on the FMA pipe too: a decision a - b + K becomes
+  // a * one + (b * mone + K), two IMADs instead of one IADD3 on the ALU pipe, which the
+  // maxima, table lookups and pushes keep busier.
+  const uint32_t mone = 0u - one;
+  const uint32_t ngo2 = ((uint32_t)(-x.go) & 0xffffu) * kOne2;  // + (-go) mod 2^16
+  const uint32_t kGtGo = kGt2 + go2;                          // gt2 against a value less go
   // Warp-scan decays: a lane's gap value falls by ext * C per lane it crosses.  The lane's
   // own chain is the maximum over its cells of H' + ext * k, less go + ext * (C/2 - 1).
   const int32_t dC = x.ext * C, dH = -x.ext * C2;
@@ -330,16 +336,17 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
     for (int q = 0; q < G; ++q) acc1[q] = 0;
     auto cell = [&](auto kt, uint32_t hd, uint32_t hu, uint32_t fu) {
       constexpr int k = decltype(kt)::value;
-      const uint32_t ho = hu * one - go2;
-      const uint32_t fo = fu * one - ext2;
-      const uint32_t fj = __vmaxu2(ho, fo);
+      // F = max(Hup - go, Fup - ext).
+      const uint32_t fj = __viaddmax_u16x2(hu, ngo2, fu * one - ext2);
       // This row's column k, after its shift.
       constexpr int sk = (D1 && ROT >= 0) ? (k + ROT + 1) % C2 : k;
       const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[sk]);  // diagonal + s + mis
       const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
+      // "F extended": fj > Hup - go; "diagonal lost": xx > dgp - mis.
       if constexpr (TB)
-        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), xx - dgp + kGtDg);
-      const uint32_t t = ext2 * (uint32_t)k + xx;
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtGo),
+                                    xx * one + (dgp * mone + kGtDg));
+      const uint32_t t = xx * one + ext2 * (uint32_t)k;
       if constexpr (k == 0)
         red = t;
       else if constexpr (k & 1)
@@ -401,7 +408,9 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
       const uint32_t xx = h[k];
       const uint32_t xo = xp * one - go2;
       if (k > 0) e = __viaddmax_u16x2(e, next2, xo);
-      if constexpr (TB) acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], gt2(e, xo), gt2(e, xx));
+      // "E extended": e > H'left - go (FMA pipe); "H from E": e > H' (ALU pipe).
+      if constexpr (TB)
+        acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], e * one + (xp * mone + kGtGo), gt2(e, xx));
       h[k] = __vmaxu2(xx, e);
       xp = xx;
     });
@@ -613,6 +622,9 @@ __device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lan
   const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
   const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
   const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;
+  const uint32_t mone = 0u - one;
+  const uint32_t ngo2 = ((uint32_t)(-x.go) & 0xffffu) * kOne2;
+  const uint32_t kGtGo = kGt2 + go2;
   const int32_t dC = x.ext * C, dH = -x.ext * C2;
   const int32_t goX = x.go + x.ext * (C2 - 1);
   const int32_t e_lane = (int32_t)kNeg16 - dC * l;
@@ -753,14 +765,13 @@ __device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lan
         hd = D1 ? hk : hdp;
         hdp = hk;
       }
-      const uint32_t ho = hu * one - go2;
-      const uint32_t fo = fu * one - ext2;
-      const uint32_t fj = __vmaxu2(ho, fo);
+      const uint32_t fj = __viaddmax_u16x2(hu, ngo2, fu * one - ext2);
       const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);
       const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
       if constexpr (TB)
-        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], gt2(fj, ho), xx - dgp + kGtDg);
-      const uint32_t t = ext2 * (uint32_t)k + xx;
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtGo),
+                                    xx * one + (dgp * mone + kGtDg));
+      const uint32_t t = xx * one + ext2 * (uint32_t)k;
       if constexpr (k == 0)
         red = t;
       else if constexpr (k & 1)
@@ -792,7 +803,9 @@ __device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lan
       const uint32_t xx = h[k];
       const uint32_t xo = xp * one - go2;
       if (k > 0) e = __viaddmax_u16x2(e, next2, xo);
-      if constexpr (TB) acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], gt2(e, xo), gt2(e, xx));
+      // "E extended": e > H'left - go (FMA pipe); "H from E": e > H' (ALU pipe).
+      if constexpr (TB)
+        acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], e * one + (xp * mone + kGtGo), gt2(e, xx));
       h[k] = __vmaxu2(xx, e);
       xp = xx;
     });

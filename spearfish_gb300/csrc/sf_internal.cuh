@@ -94,9 +94,12 @@ struct DLink {
 };
 
 // 4-warp blocks of the 16-bit register kernel resident per SM (its launch bounds), by words
-// per lane.
+// per lane: the most that compile without spills (C = 24, 28: 4 blocks in at most 128
+// registers; C = 40: 3 in 160).  Measured on config 3 with the autotuner on: 91.0 -> 87.9 ms
+// a step together with the rebalanced decision compares; one more block each spilled and
+// ran slower.
 __host__ __device__ constexpr int min_blocks16(int c2) {
-  return c2 <= 8 ? 6 : (c2 <= 10 ? 4 : (c2 <= 16 ? 3 : 2));
+  return c2 <= 8 ? 6 : (c2 <= 14 ? 4 : (c2 <= 20 ? 3 : 2));
 }
 
 // A snapshot slot of the 16-bit kernel with C2 words per lane: H words, F words (word k of
