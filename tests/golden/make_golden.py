@@ -129,6 +129,39 @@ def kats() -> list[dict]:
             "sc": ont, "band": 16, "end_bonus": 5, "xdrop": 50}, list(want[i]),
             "map/src/lib.rs:3257-3297")
     add("segment_totals", {}, [28, 21, 13, 13], "map/src/lib.rs:3293")
+    # The same example through `Mapper::segmented` (lib.rs:3294-3297): the read, the four
+    # transcripts, each hit's chain of (query start, transcript start, length) anchors
+    # (lib.rs:3245-3250), TieBreak defaults with flank_min 0 and end_bonus_cut off
+    # (lib.rs:3259-3263); costs are the negated totals.
+    add("segmented", {"read": codes(qs), "texts": [codes(t) for t in texts],
+                      "hits": [[0, [[7, 7, 3], [10, 10, 8]]], [1, [[7, 8, 3], [10, 11, 8]]],
+                               [2, [[7, 7, 3], [10, 12, 8]]], [3, [[7, 9, 3], [10, 12, 8]]]],
+                      "tb": {"flank_min": 0, "end_bonus_cut": False}},
+        [-28, -21, -13, -13], "map/src/lib.rs:3294-3297")
+    # `shared_blocks` (lib.rs:562-630): blocks as [[qs, qe], [[ts, te], ...]], None as null.
+    for chains, want, cite in (
+            ([[[2, 2, 3]], [[2, 2, 4]]], None, "map/src/lib.rs:3164"),
+            ([[[2, 4, 3], [2, 8, 4]], [[2, 9, 4]]], [[[2, 6], [[8, 12], [9, 13]]]],
+             "map/src/lib.rs:3165-3172"),
+            ([[[2, 4, 5], [4, 6, 2], [6, 8, 5], [11, 15, 2]],
+              [[2, 5, 5], [4, 7, 2], [6, 9, 5], [11, 16, 2]]],
+             [[[2, 11], [[4, 13], [5, 14]]], [[11, 13], [[15, 17], [16, 18]]]],
+             "map/src/lib.rs:3173-3190"),
+            ([[[2, 2, 5], [4, 5, 5]]], [[[2, 7], [[2, 7]]]], "map/src/lib.rs:3196-3199"),
+            ([[[2, 2, 3], [6, 4, 3]]], [[[2, 5], [[2, 5]]]], "map/src/lib.rs:3200-3203"),
+            ([[[0, 0, 1], [2, 2, 4], [2, 2, 3], [2, 2, 3], [8, 8, 2], [12, 12, 2]],
+              [[1, 2, 1], [2, 3, 3], [2, 3, 4], [7, 8, 1], [12, 15, 2]],
+              [[2, 4, 4], [2, 4, 3], [10, 12, 1], [12, 16, 2]]],
+             [[[2, 6], [[2, 6], [3, 7], [4, 8]]], [[12, 14], [[12, 14], [15, 17], [16, 18]]]],
+             "map/src/lib.rs:3207-3229"),
+            ([[[0, 0, 1], [2, 2, 4], [2, 2, 3], [2, 2, 3], [8, 8, 2], [12, 12, 2]], []], None,
+             "map/src/lib.rs:3230-3232")):
+        add("shared_blocks", {"chains": chains}, want, cite)
+    # `tail_start` (lib.rs:2935-2969) with run 15 (lib.rs:3307-3313).
+    for seq, want, cite in (("CGTCAAAAAAAAAAAAAAAGT", [4, 19], "map/src/lib.rs:3309"),
+                            ("CGAAAAAAACAAAAAAAGT", [2, 17], "map/src/lib.rs:3311"),
+                            ("CGTCAAAAAAAAAAGTCAAAA", None, "map/src/lib.rs:3312")):
+        add("tail_start", {"rest": codes(seq), "run": 15}, want, cite)
     _ = hifi
     return out
 
