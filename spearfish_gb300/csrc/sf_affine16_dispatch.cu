@@ -71,6 +71,29 @@ cudaError_t launch_affine16h(int c, bool tb, const AffLaunch& a, int grid, int b
   }
 }
 
+cudaError_t launch_affine16w_12(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16w_16(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16w_20(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16w_24(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16w_28(bool, const AffLaunch&, int, int, cudaStream_t);
+cudaError_t launch_affine16w_32(bool, const AffLaunch&, int, int, cudaStream_t);
+
+const int kAffine16WC[] = {12, 16, 20, 24, 28, 32};
+const int kAffine16WNC = 6;
+
+cudaError_t launch_affine16w(int c, bool tb, const AffLaunch& a, int grid, int block,
+                             cudaStream_t s) {
+  switch (c) {
+    case 12: return launch_affine16w_12(tb, a, grid, block, s);
+    case 16: return launch_affine16w_16(tb, a, grid, block, s);
+    case 20: return launch_affine16w_20(tb, a, grid, block, s);
+    case 24: return launch_affine16w_24(tb, a, grid, block, s);
+    case 28: return launch_affine16w_28(tb, a, grid, block, s);
+    case 32: return launch_affine16w_32(tb, a, grid, block, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_affine16_chain_4(const AffLaunch&, int, int, cudaStream_t);
 cudaError_t launch_affine16_chain_6(const AffLaunch&, int, int, cudaStream_t);
 cudaError_t launch_affine16_chain_8(const AffLaunch&, int, int, cudaStream_t);

@@ -571,6 +571,372 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
 }
 
 // ---------------------------------------------------------------------------------------
+// Two-warp passes: the same rows on 64 lanes, the two warps of a 64-thread block each holding
+// 32 lanes of C cells, for bands too wide for one warp to run at speed: a long pass is bound
+// by its own row latency (one warp's dependent chain per row), and splitting its row shortens
+// that chain.  Lane l (0..63, warp l / 32) holds offsets [l*C, l*C + C).  Per row the warps
+// exchange values through shared memory, each exchange behind a block barrier:
+//  - after pass 1 and each warp's gap scan: warp 0's scan total (the gap entering warp 1) and
+//    its last H' (left of warp 1's first cell);
+//  - after the row: warp 1's first H and F (above warp 0's last cell in the next row) and
+//    warp 0's last H (left of warp 1's first cell in the next row while lo = 0);
+//  - in rows that need a row maximum (the rebase every 64 rows, clip and X-drop, cut): each
+//    warp's maximum, so that both warps take the same decisions.
+// Every barrier sits on a path both warps take (every branch around one tests values both
+// warps hold alike), and the block is the pass's two warps alone, so a barrier is the plain
+// block barrier.  Warp 0 walks the traceback; its layout is the one-warp layout with 64 lanes
+// to a group.
+struct Team16 {
+  uint32_t nh, nf;   // warp 1's first H and F after the last row
+  uint32_t ph;       // warp 0's last H after the last row
+  uint32_t hx;       // warp 0's last H' of this row
+  int32_t s0;        // warp 0's gap total of this row
+  uint32_t v[4][2];  // per-warp values of a row's maxima and leftmost cells; the score
+  uint32_t job;
+};
+
+template <int C2, bool TB>
+__device__ __forceinline__ void pair16w(const sfk::AffLaunch& a, uint32_t jid, int lane, int w,
+                                        Team16& X) {
+  constexpr int C = 2 * C2;
+  constexpr int G = (C2 + 7) / 8;
+  constexpr int LP = 64;
+  constexpr bool kMasks = C2 <= 8;
+  const int l = 32 * w + lane;
+  const PassCtx x = make_ctx(a, jid);
+  DRes r{};
+  const int32_t m = (int32_t)x.m, n = (int32_t)x.n;
+  const Geo32 g{(x.P.flags & F_FULL) != 0, false, clamp30(x.J.below), clamp30(x.J.above), n};
+  const int32_t cut =
+      x.cuton ? (int32_t)(x.J.cut < (uint64_t)n + 1 ? x.J.cut : (uint64_t)n + 1) : INT32_MAX;
+  const int32_t kb = l * C;
+  const uint32_t one = (uint32_t)opaque_one();
+  const uint32_t go2 = (uint32_t)x.go * kOne2;
+  const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;
+  const uint32_t ext2 = (uint32_t)x.ext * kOne2;
+  const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
+  const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
+  const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;
+  const uint32_t mone = 0u - one;
+  const uint32_t ngo2 = ((uint32_t)(-x.go) & 0xffffu) * kOne2;
+  const uint32_t kGtGo = kGt2 + go2;
+  const int32_t dC = x.ext * C, dH = -x.ext * C2;
+  const int32_t goX = x.go + x.ext * (C2 - 1);
+  const int32_t e_lane = (int32_t)kNeg16 - dC * l;
+  int32_t off = -(int32_t)kBias16;
+  uint32_t h[C2], f[C2], sel[C2], smask[kMasks ? C2 : 1];
+  int32_t plo, phi;
+  g.range(0, plo, phi);
+  {
+    const int32_t w0 = phi - plo + 1;
+#pragma unroll
+    for (int k = 0; k < C2; ++k) {
+      const int32_t K = kb + k, K2 = kb + C2 + k;
+      const uint32_t lo = K < w0 ? (uint32_t)(row0_value(x, plo + K) - off) : kNeg16;
+      const uint32_t hi = K2 < w0 ? (uint32_t)(row0_value(x, plo + K2) - off) : kNeg16;
+      h[k] = pk2(lo, hi);
+      f[k] = kNeg2;
+    }
+  }
+  {
+    int32_t lo1, hi1;
+    g.range(1, lo1, hi1);
+    Win<C> win;
+    win.load(a.pool, x.J.t_word, lo1 + kb);
+#pragma unroll
+    for (int k = 0; k < C2; ++k) sel[k] = sel_byte(win.at(k)) | (sel_byte(win.at(C2 + k)) << 8);
+  }
+  int32_t Wm = -1;
+  auto set_masks = [&](int32_t W) {
+    const int32_t c = W - kb;
+#pragma unroll
+    for (int k = 0; k < (kMasks ? C2 : 1); ++k)
+      smask[k] = (c == k ? 0xffffu : 0u) | (c == C2 + k ? 0xffff0000u : 0u);
+    Wm = W;
+  };
+  // The pass's maximum of a per-lane value (slot s of this row's exchanges).
+  auto team_max = [&](uint32_t v, int s) -> uint32_t {
+    v = __reduce_max_sync(FULL, v);
+    if (lane == 0) X.v[s][w] = v;
+    __syncthreads();
+    return max(X.v[s][0], X.v[s][1]);
+  };
+  // Leftmost offset of the pass holding field v (some lane holds it).
+  auto team_leftmost = [&](uint32_t v, int s) -> uint32_t {
+    int cf = C;
+#pragma unroll
+    for (int c = C - 1; c >= 0; --c) {
+      const uint32_t u = c < C2 ? (h[c] & 0xffffu) : (h[c - C2] >> 16);
+      if (u == v) cf = c;
+    }
+    const uint32_t bal = __ballot_sync(FULL, cf < C);
+    const int src = __ffs(bal) - 1;
+    const int cs = __shfl_sync(FULL, cf, src < 0 ? 0 : src);
+    const uint32_t mine = src < 0 ? 0xffffffffu : (uint32_t)(32 * w + src) * C + (uint32_t)cs;
+    if (lane == 0) X.v[s][w] = mine;
+    __syncthreads();
+    return min(X.v[s][0], X.v[s][1]);
+  };
+  Book b;
+  uint32_t pw = m > 0 ? __ldg(a.pool + x.J.p_word) >> 2 : 0;
+  uint2* tbp = TB ? reinterpret_cast<uint2*>(a.tb + x.J.tb_word) + l : nullptr;
+  // Row 0's values at the seam, for row 1.
+  if (w == 1 && lane == 0) {
+    X.nh = h[0];
+    X.nf = f[0];
+  }
+  if (w == 0 && lane == 31) X.ph = h[C2 - 1];
+  __syncthreads();
+
+  int32_t Wc = 0, ks = 0;
+  uint32_t ms = 0;
+  bool sent = false;
+  auto row = [&](int32_t i, auto modetag) -> bool {
+    constexpr int MODE = decltype(modetag)::value;
+    constexpr bool D1 = MODE >= 1, ST = MODE == 2;
+    const int32_t lo = D1 ? i - g.below : 0, hi = ST ? i + g.above : min(i + g.above, n);
+    const int32_t W = ST ? Wc : hi - lo + 1;
+    if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + (i >> 4));
+    const uint32_t pb = 8u * (pw & 3u);
+    pw >>= 2;
+    const uint32_t ta = (mpm & 0xffu) << pb, tbl = (mpm >> 8) << pb;
+    if (D1 && i > 1) {
+      const uint32_t s0 = sel[0];
+      uint32_t nx = __shfl_down_sync(FULL, s0, 1);
+      // The column entering this warp's lane 31: the next warp's first, or past the band.
+      const uint32_t fcol = (uint32_t)(lo + 32 * (w + 1) * C - 1);
+      const uint32_t fw = __ldg(a.pool + x.J.t_word + (fcol >> 4));
+      const uint32_t far = sel_byte((fw >> (2u * (fcol & 15u))) & 3u);
+      if (lane == 31) nx = far;
+#pragma unroll
+      for (int k = 0; k + 1 < C2; ++k) sel[k] = sel[k + 1];
+      sel[C2 - 1] = __byte_perm(s0, nx, 0x2241);
+    }
+
+    uint32_t red = 0, pend = 0;
+    uint32_t acc1[G];
+#pragma unroll
+    for (int q = 0; q < G; ++q) acc1[q] = 0;
+    auto cell = [&](auto kt, uint32_t hd, uint32_t hu, uint32_t fu) {
+      constexpr int k = decltype(kt)::value;
+      const uint32_t fj = __viaddmax_u16x2(hu, ngo2, fu * one - ext2);
+      const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);
+      const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
+      if constexpr (TB)
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtGo),
+                                    xx * one + (dgp * mone + kGtDg));
+      const uint32_t t = xx * one + ext2 * (uint32_t)k;
+      if constexpr (k == 0)
+        red = t;
+      else if constexpr (k & 1)
+        pend = t;
+      else
+        red = __vimax3_u16x2(red, pend, t);
+      f[k] = fj;
+      h[k] = xx;
+    };
+    if constexpr (D1) {
+      uint32_t nH = __shfl_down_sync(FULL, h[0], 1), nF = __shfl_down_sync(FULL, f[0], 1);
+      if (lane == 31) {
+        nH = w == 0 ? X.nh : kNeg2;
+        nF = w == 0 ? X.nf : kNeg2;
+      }
+      const uint32_t upH = __byte_perm(h[0], nH, 0x5432), upF = __byte_perm(f[0], nF, 0x5432);
+      sf_unroll<C2>([&](auto kt) {
+        constexpr int k = decltype(kt)::value;
+        cell(kt, h[k], k + 1 < C2 ? h[k + 1 < C2 ? k + 1 : 0] : upH,
+             k + 1 < C2 ? f[k + 1 < C2 ? k + 1 : 0] : upF);
+      });
+    } else {
+      uint32_t pl = __shfl_up_sync(FULL, h[C2 - 1], 1);
+      if (lane == 0 && w == 1) pl = X.ph;
+      uint32_t hd = __byte_perm(pl, h[C2 - 1], 0x5432);
+      if (l == 0) hd = (hd & 0xffff0000u) | (kNeg16 - (uint32_t)x.mat - 1u);
+      sf_unroll<C2>([&](auto kt) {
+        constexpr int k = decltype(kt)::value;
+        const uint32_t hu = h[k];
+        cell(kt, hd, hu, f[k]);
+        hd = hu;
+      });
+    }
+
+    if constexpr (C2 % 2 == 0) red = __vmaxu2(red, pend);
+    const int32_t clo = (int32_t)(red & 0xffffu) - goX, chi = (int32_t)(red >> 16) - goX;
+    int32_t S = addmax(clo, dH, chi);
+    S = addmax(__shfl_up_sync(FULL, S, 1), -dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 2), -2 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 4), -4 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 8), -8 * dC, S);
+    S = addmax(__shfl_up_sync(FULL, S, 16), -16 * dC, S);
+    // Warp 0's total and last H' to warp 1: the gap entering lane 32 + j is the larger of its
+    // warp's own scan and warp 0's total decayed over j + 1 lanes.
+    if (w == 0 && lane == 31) {
+      X.s0 = S;
+      X.hx = h[C2 - 1];
+    }
+    __syncthreads();
+    int32_t Sp;
+    uint32_t pl2 = __shfl_up_sync(FULL, h[C2 - 1], 1);
+    if (w == 1) {
+      const int32_t T = X.s0;
+      S = addmax(T, -dC * (lane + 1), S);
+      Sp = __shfl_up_sync(FULL, S, 1);
+      if (lane == 0) {
+        Sp = T;
+        pl2 = X.hx;
+      }
+    } else {
+      Sp = __shfl_up_sync(FULL, S, 1);
+    }
+    const int32_t ein = l == 0 ? (int32_t)kNeg16 : max(e_lane, Sp);
+    const int32_t ehi = addmax(ein, dH, clo);
+    uint32_t e = pk2((uint32_t)ein, (uint32_t)ehi);
+    uint32_t xp = __byte_perm(pl2, h[C2 - 1], 0x5432);
+    if (l == 0) xp = (xp & 0xffff0000u) | (kNeg16 - 1u);
+
+    uint32_t acc2[G];
+#pragma unroll
+    for (int q = 0; q < G; ++q) acc2[q] = 0;
+    sf_unroll<C2>([&](auto kt) {
+      constexpr int k = decltype(kt)::value;
+      const uint32_t xx = h[k];
+      const uint32_t xo = xp * one - go2;
+      if (k > 0) e = __viaddmax_u16x2(e, next2, xo);
+      if constexpr (TB)
+        acc2[k >> 3] = push2<k & 7>(acc2[k >> 3], e * one + (xp * mone + kGtGo), gt2(e, xx));
+      h[k] = __vmaxu2(xx, e);
+      xp = xx;
+    });
+    if constexpr (TB) {
+#pragma unroll
+      for (int q = 0; q < G; ++q) tbp[q * LP] = make_uint2(acc1[q], acc2[q]);
+      tbp += G * LP;
+    }
+    const bool rebase = (i & (kRebaseRows - 1)) == 0;
+    if (x.rowmax_on || rebase) {
+      const uint32_t rmu = team_max(lane_max16(h, kb, W), 0);
+      if (x.rowmax_on) {
+        const int32_t rmax = (int32_t)rmu + off;
+        if (x.cuton && lo <= cut) {
+          int32_t rowv = rmax;
+          if (hi > cut) rowv = (int32_t)team_max(lane_max16(h, kb, cut - lo + 1), 1) + off;
+          b.cut_best = max(b.cut_best, rowv);
+        }
+        if (x.clip) {
+          if (rmax > b.clip_best) {
+            b.clip_best = rmax;
+            if (x.cell) {
+              b.ci = (uint32_t)i;
+              b.cj = (uint32_t)lo + team_leftmost(rmu, 2);
+            }
+          }
+          if (rmax < sat_sub(b.clip_best, x.P.xdrop)) {
+            r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)hi,
+                     (uint32_t)i, (uint32_t)i, band_cells(i, g.below, g.above, n)};
+            return true;
+          }
+        }
+      }
+      if (rebase) {
+        const int32_t delta = (int32_t)rmu - (int32_t)kBias16;
+        const uint32_t dd = ((uint32_t)(-delta) & 0xffffu) * kOne2;
+#pragma unroll
+        for (int k = 0; k < C2; ++k) {
+          h[k] = __viaddmax_u16x2(h[k], dd, kNeg2);
+          f[k] = __viaddmax_u16x2(f[k], dd, kNeg2);
+        }
+        off += delta;
+      }
+    }
+    if constexpr (ST) {
+      if (sent) set_word16(h, f, ks, ms);
+    } else if (W < LP * C) {
+      if constexpr (kMasks) {
+        if (W != Wm) set_masks(W);
+#pragma unroll
+        for (int k = 0; k < C2; ++k) {
+          h[k] = (h[k] & ~smask[k]) | (kNeg2 & smask[k]);
+          f[k] = (f[k] & ~smask[k]) | (kNeg2 & smask[k]);
+        }
+      } else if (l == W / C) {
+        set_neg16(h, f, W - kb);
+      }
+    }
+    plo = lo;
+    phi = hi;
+    // The seam values for the next row.
+    if (w == 1 && lane == 0) {
+      X.nh = h[0];
+      X.nf = f[0];
+    }
+    if (w == 0 && lane == 31) X.ph = h[C2 - 1];
+    __syncthreads();
+    return false;
+  };
+
+  bool stopped = false;
+  const int32_t endA = m < g.below ? m : g.below;
+  const int64_t lastB = (int64_t)n + g.below;
+  const int32_t endB = (int64_t)m < lastB ? m : (int32_t)lastB;
+  const int32_t endS = min(endB, n - g.above);
+  for (int32_t i = 1; i <= endA && !stopped; ++i)
+    stopped = row(i, std::integral_constant<int, 0>{});
+  int32_t i1 = endA + 1;
+  if (i1 <= endS) {
+    Wc = g.below + g.above + 1;
+    sent = Wc < LP * C;
+    const int32_t Ls = Wc / C, c = Wc - Ls * C;
+    ks = c < C2 ? c : c - C2;
+    ms = l == Ls ? (c < C2 ? 0xffffu : 0xffff0000u) : 0u;
+    Wm = -1;
+    for (; i1 <= endS && !stopped; ++i1) stopped = row(i1, std::integral_constant<int, 2>{});
+  }
+  for (int32_t i = i1; i <= endB && !stopped; ++i)
+    stopped = row(i, std::integral_constant<int, 1>{});
+  if (!stopped && endB < m) {
+    r = DRes{NEG, b.clip_best, b.cut_best, NEG, 0, b.ci, b.cj, (uint32_t)n, (uint32_t)(endB + 1),
+             (uint32_t)endB, band_cells(endB, g.below, g.above, n)};
+    stopped = true;
+  }
+  if (!stopped) {
+    const int32_t W = phi - plo + 1;
+    r.clip_best = b.clip_best;
+    r.cut_best = b.cut_best;
+    r.clip_i = b.ci;
+    r.clip_j = b.cj;
+    r.text_read = (uint32_t)phi;
+    r.last_row = (uint32_t)m;
+    r.rows = (uint32_t)m;
+    r.cells = band_cells(m, g.below, g.above, n);
+    if (x.mode == 2) {
+      const int32_t K = n - plo;
+      const uint32_t u = __shfl_sync(FULL, field_at(h, K % C), (K / C) & 31);
+      if (lane == 0 && w == ((K / C) >> 5)) X.v[3][0] = u;
+      __syncthreads();
+      r.score = (int32_t)X.v[3][0] + off;
+      r.score_col = (uint32_t)n;
+    } else {
+      const uint32_t rmu = team_max(lane_max16(h, kb, W), 0);
+      r.score = (int32_t)rmu + off;
+      r.score_col = (uint32_t)plo + team_leftmost(rmu, 2);
+    }
+    r.cut_score = NEG;
+    if (x.cuton && plo <= cut) {
+      const int32_t lim = min(phi, cut) - plo + 1;
+      r.cut_score = (int32_t)team_max(lane_max16(h, kb, lim), 1) + off;
+    }
+  }
+  if (w == 0) {
+    if (lane == 0) a.out[jid] = r;
+    if constexpr (TB) {
+      __syncwarp();
+      walk_lean(a, jid, tb_layout<C>(false, true, x.J, x.P.flags, LP), x.J, x.P.flags, r, lane);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // Half-warp passes: the same rows with 16 lanes to a pass and two passes to a warp, so that a
 // row's fixed costs (the gap scan, the neighbour shuffles, table and bookkeeping work) are
 // shared between the warp's two passes and a lane holds twice the cells.  Lane l of segment
@@ -935,6 +1301,21 @@ struct MinBlocks16 {
   static constexpr int value = min_blocks16(C2);
 };
 
+// Two-warp passes: a 64-thread block per pass, the pass's two warps taking jobs together.
+template <int C2, bool TB>
+__global__ void __launch_bounds__(64, 2 * MinBlocks16<C2>::value) affine16w_kernel(sfk::AffLaunch a) {
+  __shared__ Team16 X;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) X.job = atomicAdd(a.counter, 1u);
+    __syncthreads();
+    const uint32_t q = X.job;
+    if (q >= a.njobs) break;
+    pair16w<C2, TB>(a, a.order[q], lane, w, X);
+    __syncthreads();
+  }
+}
+
 template <int C2, bool TB>
 __global__ void __launch_bounds__(128, MinBlocks16<C2>::value) affine16_kernel(sfk::AffLaunch a) {
   const int lane = threadIdx.x & 31;
@@ -1003,6 +1384,15 @@ cudaError_t launch_affine16h_c(bool tb, const AffLaunch& a, int grid, int block,
     affine16h_kernel<C2, true><<<grid, block, 0, s>>>(a);
   else
     affine16h_kernel<C2, false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int C2>
+cudaError_t launch_affine16w_c(bool tb, const AffLaunch& a, int grid, int block, cudaStream_t s) {
+  if (tb)
+    affine16w_kernel<C2, true><<<grid, block, 0, s>>>(a);
+  else
+    affine16w_kernel<C2, false><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -1188,25 +1188,40 @@ std::vector<ClassChoice> tune_candidates(const ClassKey& key, int64_t blocks) {
       if (!dup) out.push_back(ClassChoice{b, lanes});
     }
   } else if (!key.wide) {
-    const bool half = key.kind == PK_AFFINE16 && key.lanes == 16;
-    const int* cs = key.kind == PK_AFFINE16 ? (half ? sfk::kAffine16HC : sfk::kAffine16C)
-                                            : sfk::kAffineC;
-    const int nc = key.kind == PK_AFFINE16 ? (half ? sfk::kAffine16HNC : sfk::kAffine16NC)
-                                           : sfk::kAffineNC;
+    // The 16-bit classes for 16, 32 and 64 lanes a pass.
+    auto classes16 = [](int lanes, const int*& cs, int& nc) {
+      cs = lanes == 16 ? sfk::kAffine16HC : (lanes == 64 ? sfk::kAffine16WC : sfk::kAffine16C);
+      nc = lanes == 16 ? sfk::kAffine16HNC : (lanes == 64 ? sfk::kAffine16WNC : sfk::kAffine16NC);
+    };
+    const int* cs = sfk::kAffineC;
+    int nc = sfk::kAffineNC;
+    if (key.kind == PK_AFFINE16) classes16(key.lanes, cs, nc);
     for (int q = 0; q < nc; ++q)
       if (cs[q] > key.c && (int)out.size() < 3) out.push_back(ClassChoice{cs[q], key.lanes});
-    // 16-bit rows: the other lane count per pass (two passes per warp, or one), its two
-    // narrowest classes that hold the group's widest row (`blocks` carries it here).
-    const int other = half ? 32 : 16;
-    const int* os = half ? sfk::kAffine16C : sfk::kAffine16HC;
-    const int no = half ? sfk::kAffine16NC : sfk::kAffine16HNC;
-    int added = 0;
-    if (key.kind == PK_AFFINE16)
-      for (int q = 0; q < no && added < 2; ++q)
-        if ((int64_t)other * os[q] >= blocks) {
-          out.push_back(ClassChoice{os[q], other});
+    // 16-bit rows: other lane counts per pass, the narrowest classes that hold the group's
+    // widest row (`blocks` carries it here) -- two passes per warp or one (16 <-> 32 lanes,
+    // two classes), and one warp or two (32 <-> 64 lanes, one class, rows over 1,280 cells).
+    // Two warps are offered for the widest rows only: timed alone a group of 1,025-1,280
+    // cell rows can run faster on them, but among the other buckets of a batch its barriers
+    // wait on busy SMs (config 3's passes over 4.8 kb: 33.5 ms a step on one warp each,
+    // 55 ms on two).
+    auto add_other = [&](int lanes, int most) {
+      const int* os;
+      int no;
+      classes16(lanes, os, no);
+      int added = 0;
+      for (int q = 0; q < no && added < most; ++q)
+        if ((int64_t)lanes * os[q] >= blocks) {
+          out.push_back(ClassChoice{os[q], lanes});
           ++added;
         }
+    };
+    if (key.kind == PK_AFFINE16) {
+      if (key.lanes == 16) add_other(32, 2);
+      if (key.lanes == 32) add_other(16, 2);
+      if (key.lanes == 32 && blocks > 32 * 40) add_other(64, 1);
+      if (key.lanes == 64) add_other(32, 1);
+    }
   }
   return out;
 }

@@ -219,6 +219,11 @@ cudaError_t launch_affine16h(int c, bool tb, const AffLaunch& a, int grid, int b
                              cudaStream_t s);
 extern const int kAffine16HC[];
 extern const int kAffine16HNC;
+// The same rows with 64 lanes to a pass: two warps of a 64-thread block (wide bands).
+cudaError_t launch_affine16w(int c, bool tb, const AffLaunch& a, int grid, int block,
+                             cudaStream_t s);
+extern const int kAffine16WC[];
+extern const int kAffine16WNC;
 // Chains of sorted texts on the 16-bit register kernel (C from kAffine16C, no traceback).
 cudaError_t launch_affine16_chain(int c, const AffLaunch& a, int grid, int block,
                                   cudaStream_t s);

@@ -93,11 +93,14 @@ bool allow16() {
   return !(env && env[0] == '0');
 }
 
-// Lanes per 16-bit pass by default: 32, or 16 (two passes per warp) with SF_AFFINE16_LANES=16
-// in the environment; the autotuner chooses per length bucket either way.
+// Lanes per 16-bit pass by default: 32 (with 64 for rows wider than 32 x 40 cells), or with
+// SF_AFFINE16_LANES in the environment 16 (two passes per warp) or 64 (two warps per pass,
+// every pass a 64-lane class holds); the autotuner chooses per length bucket either way.
 int default_lanes16() {
   const char* env = std::getenv("SF_AFFINE16_LANES");
-  return env && env[0] == '1' && env[1] == '6' ? 16 : 32;
+  if (env && env[0] == '1' && env[1] == '6') return 16;
+  if (env && env[0] == '6' && env[1] == '4') return 64;
+  return 32;
 }
 
 // Row sharing between sorted texts on the GPU: SF_SORTED_CHAINS=1 in the environment runs
@@ -115,6 +118,14 @@ bool allow_chains() {
   return env && env[0] == '1';
 }
 
+// Two-warp 16-bit passes (64 lanes) for rows wider than 32 x 40 cells: such passes are long
+// and bound by their own row latency on one warp.  SF_AFFINE16_W64=0 in the environment keeps
+// one warp a pass (the autotuner may still choose either per length bucket); read per plan.
+bool allow_w64() {
+  const char* env = std::getenv("SF_AFFINE16_W64");
+  return !(env && env[0] == '0');
+}
+
 // Kernel class of an affine or local pass: the packed 16-bit kernel when the pass fits it,
 // else the 32-bit register kernel, else (rows wider than 32 * 48 cells) the wide-row kernel.
 void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, PassKind& kind,
@@ -128,6 +139,14 @@ void classify_affine(const Pass& p, uint32_t flags, int64_t wmax, bool use16, Pa
           kind = PK_AFFINE16;
           c = sfk::kAffine16HC[q];
           lanes = 16;
+          return;
+        }
+    if ((wmax > 32 * 40 && allow_w64()) || lanes16 == 64)
+      for (int q = 0; q < sfk::kAffine16WNC; ++q)
+        if (64 * (int64_t)sfk::kAffine16WC[q] >= wmax) {
+          kind = PK_AFFINE16;
+          c = sfk::kAffine16WC[q];
+          lanes = 64;
           return;
         }
     for (int q = 0; q < sfk::kAffine16NC; ++q)
@@ -778,18 +797,18 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
   const size_t ni = items.size();
   constexpr int kT = 8;
   // Buckets in key order; within a bucket, longest work first (ties in job order).
-  // Each item's bucket first: keys pack into 18-bit codes ordered as the keys are (kind < 8,
-  // C < 128, lanes < 64), so a bit set of the codes present lists the buckets in order and a
-  // code's bucket is the number of codes below it.  Keys outside those bounds (never built)
-  // take a search instead.
+  // Each item's bucket first: keys pack into 15-bit codes ordered as the keys are (kind < 8,
+  // C < 128, lanes a power of two up to 64, coded by its log2), so a bit set of the codes
+  // present lists the buckets in order and a code's bucket is the number of codes below it.
+  // Keys outside those bounds (never built) take a search instead.
   auto& kid = S.kid;
   kid.resize(ni);
   std::vector<Key2> keys;  // the buckets' keys, in order
   {
-    constexpr uint32_t kWords = (1u << 18) / 64;
+    constexpr uint32_t kWords = (1u << 15) / 64;
     auto fits = [](const Key2& k) {
       return k.kind >= 0 && k.kind < 8 && k.c >= 0 && k.c < 128 && (k.wide & ~1) == 0 &&
-             (k.tb & ~1) == 0 && k.lanes >= 0 && k.lanes < 64;
+             (k.tb & ~1) == 0 && k.lanes >= 1 && k.lanes <= 64 && (k.lanes & (k.lanes - 1)) == 0;
     };
     auto& bits = S.code_bits;
     const size_t nt = chunks_for(ni, 4096, kT);  // the chunks below: each its own bit set
@@ -804,8 +823,9 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
           packed[k] = false;
           return;
         }
-        const uint32_t c = (uint32_t)key.kind << 15 | (uint32_t)key.c << 8 |
-                           (uint32_t)key.wide << 7 | (uint32_t)key.tb << 6 | (uint32_t)key.lanes;
+        const uint32_t c = (uint32_t)key.kind << 12 | (uint32_t)key.c << 5 |
+                           (uint32_t)key.wide << 4 | (uint32_t)key.tb << 3 |
+                           (uint32_t)__builtin_ctz((uint32_t)key.lanes);
         kid[q] = c;
         w[c >> 6] |= uint64_t(1) << (c & 63);
       }
@@ -819,7 +839,8 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
         below[w + 1] = below[w] + (uint32_t)__builtin_popcountll(x);
         for (; x; x &= x - 1) {
           const int c = (int)(w * 64 + (uint32_t)__builtin_ctzll(x));
-          keys.push_back(Key2{c >> 15, (c >> 8) & 127, (c >> 7) & 1, (c >> 6) & 1, c & 63});
+          keys.push_back(Key2{(int)(c >> 12), (int)((c >> 5) & 127), (int)((c >> 4) & 1),
+                              (int)((c >> 3) & 1), 1 << (c & 7)});
         }
       }
       parallel_chunks(ni, 4096, kT, [&](size_t q0, size_t q1, int) {
@@ -971,8 +992,10 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
       const uint64_t wpb = (uint64_t)b.block / 32;
       b.grid = (int)std::min<uint64_t>((warps + wpb - 1) / wpb, (uint64_t)ctx->sms * (2048 / b.block));
     } else {
-      b.block = 128;
-      const uint64_t per_block = b.lanes == 16 ? 8 : 4;  // passes (chains) a 4-warp block holds
+      // Two-warp passes: one pass per 64-thread block; otherwise a 4-warp block holds 4
+      // passes (chains), or 8 with 16 lanes a pass.
+      b.block = b.lanes == 64 ? 64 : 128;
+      const uint64_t per_block = b.lanes == 64 ? 1 : (b.lanes == 16 ? 8 : 4);
       const uint64_t blocks = (b.count + per_block - 1) / per_block;
       const uint64_t cap = b.wide ? (uint64_t)ctx->sms * 2 : (uint64_t)ctx->sms * 16;
       b.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, cap));
@@ -1257,6 +1280,8 @@ int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* ev
       al.snap = P->d_snap.as<uint32_t>();
       if (b.kind == PK_CHAIN16)
         CK(sfk::launch_affine16_chain(b.c, al, b.grid, b.block, bs));
+      else if (b.kind == PK_AFFINE16 && b.lanes == 64)
+        CK(sfk::launch_affine16w(b.c, b.tb, al, b.grid, b.block, bs));
       else if (b.kind == PK_AFFINE16 && b.lanes == 16)
         CK(sfk::launch_affine16h(b.c, b.tb, al, b.grid, b.block, bs));
       else if (b.kind == PK_AFFINE16)
@@ -1569,6 +1594,7 @@ uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_byte
   uint64_t b = pool_bytes + 256 * 4 + 4096;
   uint64_t scratch = 0;
   const bool use16 = allow16();
+  const int lanes16 = default_lanes16();
   for (const Pass& p : passes) {
     b += (uint64_t)(p.m + p.n + 34) / 4 + 40 + 200;
     if (p.kind == PK_MYERS) continue;
@@ -1579,9 +1605,9 @@ uint64_t plan_bytes_estimate(const std::vector<Pass>& passes, uint64_t pool_byte
     bool wide = false;
     PassKind kind = PK_AFFINE;
     int ln = 32;
-    classify_affine(p, flags, wmax, use16, kind, c, wide, ln);
+    classify_affine(p, flags, wmax, use16, kind, c, wide, ln, lanes16);
     if (p.want_cigar && p.kind != PK_LOCAL) {
-      b += (uint64_t)p.m * tb_row_words(c, wide ? wide_chunks(c, wmax) : 1) * 4;
+      b += (uint64_t)p.m * tb_row_words(c, wide ? wide_chunks(c, wmax) : 1) * 4 * ln / 32;
       b += 2 * ((uint64_t)p.m + p.n + 2) * 4;
     }
     if (wide) scratch = std::max<uint64_t>(scratch, (uint64_t)wide_chunks(c, wmax) * 32 * c);

@@ -28,7 +28,7 @@ struct Pos {
 struct TbLayout {
   int32_t C, C2, TG;
   bool wide, p16;
-  int32_t lanes;  // lanes of a pass: 32, or 16 for the half-warp 16-bit rows
+  int32_t lanes;  // lanes of a pass: 32; 16 for the half-warp, 64 for the two-warp 16-bit rows
   uint32_t row;   // word pairs per row
 
   __device__ __forceinline__ Pos at(int32_t K) const {
@@ -39,17 +39,19 @@ struct TbLayout {
     p.c = r - p.L * C;
     return p;
   }
+  // Lanes wrap into the next chunk only in wide rows; a register row's lanes (16, 32 or 64
+  // of them) hold its whole band.
   __device__ __forceinline__ void move(Pos& p, int32_t delta) const {
     p.c += delta;
     if (p.c < 0) {
       p.c += C;
-      if (--p.L < 0) {
+      if (--p.L < 0 && wide) {
         p.L += 32;
         --p.qc;
       }
     } else if (p.c >= C) {
       p.c -= C;
-      if (++p.L >= 32) {
+      if (++p.L >= 32 && wide) {
         p.L -= 32;
         ++p.qc;
       }

@@ -53,13 +53,14 @@ class Jobs:
                 jobs[q][k] = v
         return jobs
 
-    def run(self, ctx, scores, int16=True, lanes=32):
-        """Runs the jobs in one plan (16-bit passes on `lanes` lanes each where they fit);
-        returns the output and the bucket kinds it used."""
-        old = os.environ.get("SF_AFFINE16")
-        old_l = os.environ.get("SF_AFFINE16_LANES")
-        os.environ["SF_AFFINE16"] = "1" if int16 else "0"
-        os.environ["SF_AFFINE16_LANES"] = str(lanes)
+    def run(self, ctx, scores, int16=True, lanes=32, w64=True):
+        """Runs the jobs in one plan (16-bit passes on `lanes` lanes each where they fit; with
+        w64, rows wider than 32 x 40 cells on two warps); returns the output and the bucket
+        kinds it used (affine16h: 16 lanes a pass, affine16w: 64)."""
+        env = {"SF_AFFINE16": "1" if int16 else "0", "SF_AFFINE16_LANES": str(lanes),
+               "SF_AFFINE16_W64": "1" if w64 else "0"}
+        old = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
         try:
             pool = self.pool.build()
             jobs = self.jobs()
@@ -68,12 +69,14 @@ class Jobs:
                 plan.upload(pool)
                 plan.execute()
                 out = plan.download()
-                kinds = {(b["kind"], b["c"]) if b["lanes"] == 32 or b["kind"] != "affine16"
-                         else ("affine16h", b["c"]) for b in json.loads(plan.describe())["buckets"]}
+                name = {16: "affine16h", 32: "affine16", 64: "affine16w"}
+                kinds = {(b["kind"], b["c"]) if b["kind"] != "affine16"
+                         else (name[b["lanes"]], b["c"])
+                         for b in json.loads(plan.describe())["buckets"]}
             finally:
                 plan.close()
         finally:
-            for k, v in (("SF_AFFINE16", old), ("SF_AFFINE16_LANES", old_l)):
+            for k, v in old.items():
                 if v is None:
                     del os.environ[k]
                 else:
@@ -159,13 +162,17 @@ def test_every_class(ctx):
             J.add(None, p=p, t=t, kind=2, band=band, window=w, xdrop=xd,
                   end_bonus=int(rng.integers(0, 9)), want_cigar=1 - rep, sc_index=sci)
     scores = (R.ONT, R.HIFI)
-    out, kinds = J.run(ctx, scores)
+    out, kinds = J.run(ctx, scores, w64=False)
     classes = {c for k, c in kinds if k == "affine16"}
     assert classes >= {4, 8, 16, 32, 48, 64}, sorted(classes)
     _check(J, out, scores)
     out32, kinds32 = J.run(ctx, scores, int16=False)
-    assert not any(k == "affine16" for k, _ in kinds32)
+    assert not any(k.startswith("affine16") for k, _ in kinds32)
     _same(out, out32)
+    # By default the rows wider than 32 x 40 cells run on two warps: the same results.
+    outw, kindsw = J.run(ctx, scores)
+    assert {c for k, c in kindsw if k == "affine16w"} >= {24, 32}, sorted(kindsw)
+    _same(out, outw)
 
 
 def test_scores_near_the_bound(ctx):
@@ -240,3 +247,83 @@ def test_half_warp_passes(ctx):
     _check(J, out, scores)
     out32, _ = J.run(ctx, scores, lanes=32)
     _same(out, out32)
+
+
+def test_two_warp_passes(ctx):
+    """Two warps per pass (64 lanes): every two-warp class, with every 16-bit pass routed to
+    them (SF_AFFINE16_LANES=64) -- short and empty passes, passes whose band starts at column
+    0 for many rows, Global and Prefix with CIGARs, X-drop stops, clip cells and end bonuses --
+    identical to one warp per pass and to the oracle."""
+    rng = np.random.default_rng(1606)
+    J = Jobs()
+    for band in (3, 40, 150, 300, 380, 420, 500, 620, 700, 820, 900, 1000):
+        for rep in range(3):
+            m = int(rng.integers(max(20, band // 2), 2 * band + 1500))
+            p, t = R.rand_pair(m, int(rng.integers(3, 15)), int(rng.integers(1, 2 ** 62)))
+            mode = R.GLOBAL if rep != 1 else R.PREFIX
+            sci = int(rng.integers(0, 2))
+            J.add(None, p=p, t=t, kind=1, mode=mode, band=band, want_cigar=rep != 2,
+                  sc_index=sci)
+            w = len(t) + int(rng.integers(0, 100))
+            xd = int(rng.integers(10, 200)) if rng.random() < 0.7 else R.I32_MAX
+            J.add(None, p=p, t=t, kind=2, band=band, window=w, xdrop=xd,
+                  end_bonus=int(rng.integers(0, 9)), want_cigar=rep % 2, sc_index=sci)
+    for m in (0, 1, 5, 70):  # short and empty patterns among long ones
+        p, t = R.rand_pair(m, 5, int(rng.integers(1, 2 ** 62)))
+        J.add(None, p=p, t=t, kind=1, mode=R.GLOBAL, band=600, want_cigar=1)
+    # Substitutions only (m = n): rows of exactly 2 * band + 1 cells, one band per class
+    # (64 lanes x 12, 16, 20, 24, 28, 32 cells).
+    for band in (300, 450, 600, 700, 830, 950):
+        p = rng.integers(0, 4, 2 * band + 900)
+        t = p.copy()
+        hit = rng.random(t.size) < 0.08
+        t[hit] = (t[hit] + 1) & 3
+        J.add(None, p=p.tolist(), t=t.tolist(), kind=1, mode=R.GLOBAL, band=band,
+              want_cigar=1)
+    # A long pass of 12 kb whose maximum wanders (rebases on both warps).
+    q = rng.integers(0, 4, 12000).tolist()
+    t = R.mutate(q, R.rand_edits(rng, 1200, 12000))
+    J.add(None, p=q, t=t, kind=1, mode=R.GLOBAL, band=560, want_cigar=1)
+    J.add(None, p=q, t=t, kind=2, band=560, window=len(t) + 40, xdrop=150, end_bonus=5,
+          want_cigar=1)
+    scores = (R.ONT, R.HIFI)
+    out, kinds = J.run(ctx, scores, lanes=64)
+    two = {c for k, c in kinds if k == "affine16w"}
+    assert two >= {12, 16, 20, 24, 28, 32}, sorted(kinds)
+    assert not any(k == "affine16" for k, _ in kinds), sorted(kinds)
+    _check(J, out, scores)
+    out32, kinds32 = J.run(ctx, scores, lanes=32, w64=False)
+    assert not any(k == "affine16w" for k, _ in kinds32)
+    _same(out, out32)
+
+
+def test_two_warp_sorted_cut(ctx):
+    """Cut maxima (both warps' row maxima up to the cut), bonuses and X-drop through the
+    sorted-texts entry points on two-warp passes."""
+    gpu = R.GpuImpl()
+    rng = np.random.default_rng(1607)
+    old = os.environ.get("SF_AFFINE16_LANES")
+    os.environ["SF_AFFINE16_LANES"] = "64"
+    try:
+        for _ in range(4):
+            base = rng.integers(0, 4, int(rng.integers(800, 2500))).tolist()
+            p = R.mutate(base, R.rand_edits(rng, int(rng.integers(0, 80)), len(base)))
+            variants = [(int(rng.integers(0, len(base))),
+                         rng.integers(0, 4, int(rng.integers(0, 80))).tolist(),
+                         int(rng.integers(0, 200))) for _ in range(int(rng.integers(1, 5)))]
+            texts = R.sorted_texts(base, variants)
+            band, xd, bonus = int(rng.integers(200, 700)), int(rng.integers(20, 300)), \
+                int(rng.integers(0, 8))
+            w = max(len(t) for t in texts) + 40
+            c = min(len(t) for t in texts) - int(rng.integers(0, 100))
+            for args in ((bonus, xd, False, w, None, True, False),
+                         (bonus, xd, False, w, max(c, 0), True, True),
+                         (bonus, xd, True, w, max(c, 0), False, True)):
+                got = gpu.affine_extend_sorted_cut_bonus(p, texts, R.ONT, band, *args)
+                want = O.affine_extend_sorted_cut_bonus(p, texts, R.ONT, band, *args)
+                assert got == want, args
+    finally:
+        if old is None:
+            del os.environ["SF_AFFINE16_LANES"]
+        else:
+            os.environ["SF_AFFINE16_LANES"] = old
