@@ -52,7 +52,9 @@ GOLD = {"c1": "myers-infix-10k", "c2": "affine-global-band128-cigar-20k",
 # config-2 pairs (align.rs:957-982; window x + 20 + x / 10, X-drop 50, end bonus 5,
 # map/src/lib.rs:2101, 235-239), and config 1 with each pair capped at its distance + 16.
 VARIANTS = {("c2", "window"): "affine-extend-window-band128-xdrop50",
-            ("c1", "kslack"): "myers-infix-10k-cap-d+16"}
+            ("c1", "kslack"): "myers-infix-10k-cap-d+16",
+            ("c1", "kdecoy"): "myers-global-10k-decoys-cap160"}
+DECOY_K = 160  # 16% of the 1 kb queries: the unrelated texts' distances are ~3x that
 WINDOW = (20, 10, 50, 5)  # pad, pad_div, xdrop, end bonus
 K_SLACK = 16
 NONE32 = 0xFFFFFFFF
@@ -175,6 +177,13 @@ def workload(cfg: str, scale: float, cigar: bool = True, variant: str = "base"):
     from spearfish_gb300 import workloads as W
     if cfg == "c1":
         w = W.config1(int(10_000 * scale))
+        if variant == "kdecoy":
+            # The tie-break's rejected candidates: Global distances capped at DECOY_K against
+            # unrelated texts (a capped pair stops once a column is wholly past its cap).
+            w = W.decoys(w)
+            jobs = make_jobs(B, w, B.JOB_MYERS, 2, False)
+            jobs["k"] = DECOY_K
+            return w.pool, jobs, [w], "myers"
         return w.pool, make_jobs(B, w, B.JOB_MYERS, 0, False), [w], "myers"
     if cfg == "c2":
         w = W.config2(int(20_000 * scale))
@@ -207,7 +216,9 @@ def cpu_baseline(cfg, pairs_list, seconds: float, threads: int, variant: str = "
     level = O.set_level(1)  # NEON rows where the host has them (the reference's level there)
     w = pairs_list[-1]
     kind = 0 if cfg == "c1" else (2 if variant == "window" else 1)
-    mode = 0 if cfg == "c1" else (1 if variant == "window" else 2)
+    mode = (2 if variant == "kdecoy" else 0) if cfg == "c1" else (1 if variant == "window" else 2)
+    if variant == "kdecoy":
+        caps = np.full(len(pairs_list[-1]), DECOY_K, np.uint32)
     total_cells, total_t, done = 0, 0.0, 0
     idx = np.arange(len(w))
     rng = np.random.default_rng(7)
@@ -419,7 +430,10 @@ def plain_rate(cfg, pairs_list, n, variant="base", cigar=True):
     for q in range(n):
         if cfg in ("c1", "c3"):
             my = pairs_list[0]
-            A.distance(my.pattern(q), my.text(q), A.Mode.Infix)
+            if variant == "kdecoy":
+                A.distance(my.pattern(q), my.text(q), A.Mode.Global, DECOY_K)
+            else:
+                A.distance(my.pattern(q), my.text(q), A.Mode.Infix)
             my_cells += int(my.m[q]) * int(my.n[q])
             if cfg == "c1":
                 continue
@@ -450,7 +464,9 @@ def parity_check(cfg, pairs_list, res, ops, checked, threads) -> dict:
     n_my = len(pairs_list[0]) if cfg == "c3" else 0
     bad = 0
     if checked["myers"] is not None:
-        bad += int((res["distance"][idx].astype(np.int64) != checked["myers"]).sum())
+        got = res["distance"][idx].astype(np.int64)
+        got[got == NONE32] = -1  # None on both sides
+        bad += int((got != checked["myers"]).sum())
     if checked["affine"] is not None:
         bad += int((res["score"][n_my + idx].astype(np.int64) != checked["affine"]).sum())
     out = {"against": "oracle (C restatement of align.rs)", "pairs_checked": int(len(idx)),
@@ -719,9 +735,10 @@ def main():
     ap.add_argument("--plain-pairs", type=int, default=200)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cigar", type=int, default=1, help="c2/c3: traceback + CIGAR (1) or score only (0)")
-    ap.add_argument("--variant", default="base", choices=["base", "window", "kslack"],
+    ap.add_argument("--variant", default="base", choices=["base", "window", "kslack", "kdecoy"],
                     help="c2: window = the mapper's windowed read-end extension; "
-                         "c1: kslack = each pair capped at its distance + 16")
+                         "c1: kslack = each pair capped at its distance + 16; "
+                         "c1: kdecoy = Global distances capped at 160 against unrelated texts")
     ap.add_argument("--tune", type=int, default=None,
                     help="autotune the length buckets' kernel classes first (default: on)")
     args = ap.parse_args()

@@ -181,6 +181,7 @@ struct sf_plan {
   // Per pass: index in its kind's device arrays.
   std::vector<uint32_t> slot;
   uint32_t n_aff = 0, n_my = 0, n_walk = 0;
+  bool myers_kcut = false;  // a Myers pass is Global or Prefix with k < m + n
   std::vector<Bucket> buckets;
   uint64_t tb_words = 0, ops_words = 0, scratch_cells = 0;
   int wide_warps = 0;

@@ -237,6 +237,7 @@ struct MyersLaunch {
   const uint32_t* pool;
   uint32_t* out;
   int lanes;  // lanes per pair (power of two <= 32)
+  int kcut;   // some pair is Global or Prefix with k < m + n: stop pairs early (see kernel)
 };
 cudaError_t launch_myers(int blocks_per_lane, const MyersLaunch& a, int grid, int block,
                          cudaStream_t s);

@@ -6,10 +6,19 @@
 // a diagonal pipeline: at step t lane l processes column t - l, taking the delta (and the
 // column's text base) that lane l - 1 produced at step t - 1 through one __shfl_up per step.
 //
-// Every block of every column is computed (no Ukkonen cutoff): the reference's cutoff is
+// Every block of every column is computed (no Ukkonen band): the reference's cutoff is
 // exact whenever the distance is <= k and reports None otherwise (align.rs:87-168, pinned by
 // its tests `random_vs_naive` / `related_vs_naive`), so comparing the full-column distance
-// with k gives the same Option<u32>.
+// with k gives the same Option<u32>.  The band's skipped blocks would save no time here: the
+// lanes holding them still step every column their upper neighbours step.
+//
+// What does save time is the end of a capped Global or Prefix pair (KC): once every cell of
+// a column exceeds k -- row 0 holds the column index there, and each block's bottom row is
+// at least k + 64, so its 64 rows exceed k -- every later cell does too (every path to a
+// later column crosses this one), and the pair's answer is fixed: None (Global) or the best
+// so far (Prefix).  Each lane tracks its blocks' bottom-row scores; the verdict for a column
+// travels down the segment with the column's pipeline payload, and the warp stops when every
+// segment has its verdict or has run out of text.  Infix pairs never stop (row 0 is 0).
 #include <type_traits>
 #include <utility>
 
@@ -65,7 +74,7 @@ __device__ __forceinline__ void myers_step(uint64_t& pv, uint64_t& mv, uint64_t 
   neg = no;
 }
 
-template <int B>
+template <int B, bool KC>
 __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     myers_kernel(sfk::MyersLaunch a) {
   constexpr bool SMEM = B > 4;
@@ -101,6 +110,11 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     uint64_t pl0[SMEM ? 1 : B], pl1[SMEM ? 1 : B];
     uint64_t pv[B], mv[B];
     uint32_t ob[B], osub[B];
+    // KC: each block's bottom-row score in this lane's current column (D[i][0] = i), and
+    // the threshold a block must reach for all its 64 rows to exceed k.
+    int32_t sb[KC ? B : 1];
+    const int64_t kk = (int64_t)min((uint64_t)J.k, (uint64_t)m + (uint64_t)n);
+    const int64_t thr = kk + 64;
 #pragma unroll
     for (int bb = 0; bb < B; ++bb) {
       const uint32_t b = (uint32_t)l * B + bb;
@@ -138,6 +152,7 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
       }
       pv[bb] = ~0ull;
       mv[bb] = 0;
+      if constexpr (KC) sb[bb] = has && b < blocks ? (int32_t)min((b + 1) * 64u, m) : INT32_MAX / 2;
       ob[bb] = b == last_block ? last_bit : 63u;
       osub[bb] = ob[bb] >= 32 ? ob[bb] - 32 : 0u;
     }
@@ -147,9 +162,10 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     const bool owner = has && m > 0 && (uint32_t)l == last_block / B;
     const int own_bb = (int)(last_block % B);
     int score = (int)m, best = (int)m;
-    int steps = has && m > 0 ? (int)n + P - 1 : 0;
-    steps = __reduce_max_sync(FULL, steps);
-    uint32_t payload = 0;  // (text code << 2) | (pos << 1) | neg
+    const int seg_steps = has && m > 0 ? (int)n + P - 1 : 0;
+    const int steps = __reduce_max_sync(FULL, seg_steps);
+    uint32_t payload = 0;  // (column past k << 4) | (text code << 2) | (pos << 1) | neg
+    bool dead = false;     // KC, the segment's last lane: a column wholly past k went by
     uint32_t tw = 0;       // the text word holding base t + 1 (used by lane 0)
     const bool glob = J.mode == 2;
     // One step of the pipeline.  Lanes keep their state only while they are past the fill
@@ -176,7 +192,7 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
       } else {
         c0 = (tw >> (2 * K)) & 3u;
       }
-      const uint32_t c = l == 0 ? c0 : (in >> 2);
+      const uint32_t c = l == 0 ? c0 : ((in >> 2) & 3u);
       uint32_t pos = l == 0 ? (uint32_t)top : (in >> 1) & 1u;
       uint32_t neg = l == 0 ? 0u : in & 1u;
       // eq(c) from the bit planes: both code bits equal c's.
@@ -195,16 +211,36 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
           if (j >= 0) {
             pv[bb] = p2;
             mv[bb] = m2;
+            if constexpr (KC) sb[bb] += (int32_t)pos - (int32_t)neg;
           }
         } else {
           myers_step(pv[bb], mv[bb], eq, pos, neg, ob[bb], osub[bb]);
+          if constexpr (KC) sb[bb] += (int32_t)pos - (int32_t)neg;
         }
         hlast = bb == own_bb ? (int)pos - (int)neg : hlast;
       }
       score += live ? hlast : 0;
       best = min(best, score);
-      payload = (c << 2) | (pos << 1) | neg;
+      uint32_t past = 0;
+      if constexpr (KC) {
+        // Column j wholly past k down to this lane's blocks: row 0 (lane 0: D[0][j + 1] =
+        // j + 1) and every block above, as the lane before found; then this lane's blocks.
+        bool ex = l == 0 ? (int64_t)t + 1 > kk : ((in >> 4) & 1u) != 0;
+#pragma unroll
+        for (int bb = 0; bb < B; ++bb) ex = ex && sb[bb] >= thr;
+        ex = ex && live;
+        if (ex && l == P - 1) dead = true;
+        past = ex ? 16u : 0u;
+      }
+      payload = past | (c << 2) | (pos << 1) | neg;
     };
+    // KC: every segment has its column past k, or has stepped through its text.
+    auto all_done = [&](int t) -> bool {
+      const uint32_t bal = __ballot_sync(FULL, dead);
+      const bool sd = ((bal >> (seg * P + P - 1)) & 1u) != 0;
+      return __all_sync(FULL, sd || t >= seg_steps);
+    };
+    bool stop = false;
     using kAny = std::integral_constant<int, -1>;
     const int fill = steps < P - 1 ? steps : P - 1;
     int t = 0;
@@ -214,12 +250,28 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
     if constexpr (!SMEM) {
       for (; t < steps && ((t + 1) & 15) != 0; ++t) step(t, std::false_type{}, kAny{});
       for (; t + 16 <= steps; t += 16) {
+        if constexpr (KC) {
+          if (all_done(t)) {
+            stop = true;
+            break;
+          }
+        }
         if ((uint32_t)(t + 1) <= n) tw = __ldg(a.pool + J.t_word + ((uint32_t)(t + 1) >> 4));
         sf_unroll16([&](auto kt) { step(t + decltype(kt)::value, std::false_type{}, kt); });
       }
     }
-    for (; t < steps; ++t) step(t, std::false_type{}, kAny{});
+    for (; t < steps && !stop; ++t) {
+      if constexpr (KC) {
+        if ((t & 15) == 0 && all_done(t)) break;
+      }
+      step(t, std::false_type{}, kAny{});
+    }
     if (glob) best = score;
+    if constexpr (KC) {
+      // A segment whose column went past k: Global ends past k; Prefix keeps its best.
+      const uint32_t bal = __ballot_sync(FULL, dead);
+      if (((bal >> (seg * P + P - 1)) & 1u) && glob) best = INT32_MAX;
+    }
     if (has) {
       if (m == 0) {
         if (l == 0) {
@@ -237,7 +289,10 @@ __global__ void __launch_bounds__(B <= 4 ? 128 : (B <= 8 ? 64 : 32))
 template <int B>
 cudaError_t launch_b(const sfk::MyersLaunch& a, int grid, int block, cudaStream_t s) {
   const size_t sm = B > 4 ? (size_t)(block / 32) * 32 * B * 4 * sizeof(uint64_t) : 0;
-  myers_kernel<B><<<grid, block, sm, s>>>(a);
+  if (a.kcut)
+    myers_kernel<B, true><<<grid, block, sm, s>>>(a);
+  else
+    myers_kernel<B, false><<<grid, block, sm, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -113,6 +113,13 @@ bool batch_segments_on() {
   return !(e && e[0] == '0');
 }
 
+// Capped Global and Prefix Myers pairs stop at the first column wholly past their cap
+// (sf_myers.cu); SF_MYERS_STOP=0 in the environment runs them to the end (same results).
+bool allow_myers_stop() {
+  const char* env = std::getenv("SF_MYERS_STOP");
+  return !(env && env[0] == '0');
+}
+
 bool allow_chains() {
   const char* env = std::getenv("SF_SORTED_CHAINS");
   return env && env[0] == '1';
@@ -584,6 +591,7 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
   has_item.resize(np);
   constexpr int kMaxThreads = 8;
   uint64_t scratch_max[kMaxThreads] = {};
+  bool kcut[kMaxThreads] = {};
   // Descriptors of passes [q0, q1), each written at its slot.
   auto describe = [&](size_t q0, size_t q1, int worker) {
     // The tune table's answers, memoised per class (a batch has few classes).
@@ -619,6 +627,7 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
         m.n = p.n;
         m.mode = p.mode;
         m.k = p.k;
+        if (p.mode != SF_INFIX && (uint64_t)p.k < (uint64_t)p.m + p.n) kcut[worker] = true;
         per[q] = {Key2{PK_MYERS, b, 0, 0, lanes},
                   Item{sl, (uint64_t)p.n, ((uint64_t)p.n + (uint64_t)lanes) * (4u * (uint64_t)b + 4u)}};
         has_item[q] = 1;
@@ -676,6 +685,7 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
     }
   };
   parallel_chunks(np, 2048, kMaxThreads, describe);
+  P->myers_kcut = allow_myers_stop() && std::any_of(kcut, kcut + kMaxThreads, [](bool v) { return v; });
   uint64_t scratch_cells = 0;
   for (int w = 0; w < kMaxThreads; ++w) scratch_cells = std::max(scratch_cells, scratch_max[w]);
   P->scratch_cells = scratch_cells;
@@ -1257,6 +1267,7 @@ int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* ev
       ml.pool = P->d_pool.as<uint32_t>();
       ml.out = P->d_mout.as<uint32_t>();
       ml.lanes = b.lanes;
+      ml.kcut = P->myers_kcut ? 1 : 0;
       CK(sfk::launch_myers(b.c, ml, b.grid, b.block, bs));
     } else {
       sfk::AffLaunch al;

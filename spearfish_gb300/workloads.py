@@ -133,6 +133,15 @@ def config1(pairs: int = 10_000, seed: int = 1) -> Pairs:
     return _assemble(ps, ts, np.zeros(pairs), "c1")
 
 
+def decoys(w: Pairs, seed: int = 11) -> Pairs:
+    """w's patterns against unrelated texts of the same lengths: the candidates a tie-break's
+    capped Global or Prefix distance call rejects."""
+    rng = np.random.default_rng(seed)
+    ps = [w.pattern(q) for q in range(len(w))]
+    ts = [rng.integers(0, 4, int(w.n[q]), dtype=np.uint8) for q in range(len(w))]
+    return _assemble(ps, ts, w.band, w.name + "-decoys")
+
+
 def config2(pairs: int = 20_000, seed: int = 2, m: int = 2000, band: int = 128) -> Pairs:
     rng = np.random.default_rng(seed)
     ps, ts = [], []
