@@ -28,6 +28,8 @@ def run(*args):
     (("--config", "c2", "--variant", "window", "--scale", "0.002"),
      "affine-extend-window-band128-xdrop50-cigar"),
     (("--config", "c1", "--variant", "kslack", "--scale", "0.002"), "myers-infix-10k-cap-d+16"),
+    (("--config", "c1", "--variant", "kdecoy", "--scale", "0.002"),
+     "myers-global-10k-decoys-cap160"),
     (("--config", "c2", "--scale", "0.002", "--cigar", "0"), "affine-global-band128-score-20k"),
 ])
 def test_reference_arm_variants(args, workload):
