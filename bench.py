@@ -349,12 +349,14 @@ def serve_measure(seconds: float, slots: int, use_store: bool, rank: int, local:
 
         th = threading.Thread(target=feeder)
         th.start()
-        lat, cells, t_last = [], 0, t0
+        lat, qlat, rlat, cells, t_last = [], [], [], 0, t0
         for q in range(len(batches)):
             while tickets[q] is None:
                 time.sleep(0.0002)
             out, st = srv.wait(tickets[q])
             lat.append(st.total_ms)
+            qlat.append(st.queue_ms)
+            rlat.append(st.run_ms)
             cells += st.cells
             t_last = time.perf_counter()
         th.join()
@@ -367,6 +369,8 @@ def serve_measure(seconds: float, slots: int, use_store: bool, rank: int, local:
                 "offered_reads_per_s": reads / span if span > 0 else None,
                 "served_reads_per_s": reads / wall,
                 "submit_late_ms_max": 1e3 * max(late),
+                "queue_p99_ms": pct(qlat, 99), "run_p50_ms": pct(rlat, 50),
+                "run_p99_ms": pct(rlat, 99),
                 "sustained_gcups": cells / wall / 1e9, "wall_s": wall,
                 "latency": "submit to results on the host (sf_server_submit .. sf_server_wait)"}
         # Saturation: every batch submitted at once.

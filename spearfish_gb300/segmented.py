@@ -14,7 +14,8 @@ texts in sorted order, lib.rs:1363-1445) -- then all calls run in one device bat
 results.  The results equal the reference's read by read.
 
 Scope: parsed reads without raw read ends (the reference's `raw = None` path: no raw
-midpoints, no templated tails), and `affine_within = None` (the reference default).
+midpoints, no templated tails).  With `affine_within` the batch runs in two device
+launches: the unit-cost (Myers) calls, then the affine calls they select.
 Sequences are byte codes (A0 C1 G2 T3)."""
 from __future__ import annotations
 
@@ -32,9 +33,11 @@ MODE_PREFIX, MODE_GLOBAL = 1, 2
 @dataclass(frozen=True)
 class TieBreak:
     """The TieBreak fields `segmented` reads, with the reference's defaults (lib.rs:222-266).
-    affine: (mat, mis, open, ext) or None (unit costs, Myers with `cap`)."""
+    affine: (mat, mis, open, ext) or None (unit costs, Myers with `cap`); affine_within: with
+    affine scores, only texts within that many edits of the segment's best get one."""
     cap: int = 16
     affine: Optional[tuple] = (2, 4, 4, 2)
+    affine_within: Optional[int] = None
     lambda_: float = 1.0
     kappa: float = 6.0
     band: int = 16
@@ -150,11 +153,14 @@ def _count_other(t: np.ndarray, frm: int, code: int) -> int:
 
 
 class _Plan:
-    """DP calls of a batch, filled in when the batch has run."""
+    """DP calls of a batch, filled in when the batch has run: the unit-cost (Myers) calls run
+    first, then `stage2` turns their results into the affine calls that depend on them
+    (`affine_within`), then the sorted affine calls run."""
 
     def __init__(self):
         self.sorted: list = []
         self.banded: list = []
+        self.stage2: list = []
         self.sorted_out: list = []
         self.banded_out: list = []
 
@@ -168,7 +174,8 @@ def _seg(P: _Plan, tb: TieBreak, texts: list, read: np.ndarray, mode: int, rev: 
     n = len(texts)
     if all(np.array_equal(texts[0], t) for t in texts[1:]):
         return None
-    if mode == MODE_GLOBAL and len(read) == 0 and tb.affine is not None:
+    if mode == MODE_GLOBAL and len(read) == 0 and tb.affine is not None and \
+            tb.affine_within is None:
         # An insertion-only global gap costs by its length alone (lib.rs:1320-1332).
         _, _, opn, ext = tb.affine
         d = [opn + ext * len(t) if len(t) else 0 for t in texts]
@@ -202,24 +209,59 @@ def _seg(P: _Plan, tb: TieBreak, texts: list, read: np.ndarray, mode: int, rev: 
     for k, u in enumerate(uniq):
         place[u] = k
     rep = [place[d] for d in rep0]
-    tx = [decoded[u] for u in uniq]
+    tx_all = [decoded[u] for u in uniq]
     diag = mode == MODE_PREFIX and tb.clip_ends and tb.end_diagonal
-    call = {"read": rd, "texts": tx, "band": tb.band}
-    if mode == MODE_PREFIX and tb.clip_ends:
-        window = max(tb.window(len(rd)), max(len(t) for t in tx))
-        call.update(kind=1, end_bonus=tb.end_bonus, xdrop=tb.xdrop, diagonal=diag,
-                    window=window, cut=cut, track_cut=tb.flank_min > 0,
-                    bonus_within_cut=tb.end_bonus_cut)
+
+    def sorted_call(tx):
+        call = {"read": rd, "texts": tx, "band": tb.band}
+        if mode == MODE_PREFIX and tb.clip_ends:
+            window = max(tb.window(len(rd)), max(len(t) for t in tx))
+            call.update(kind=1, end_bonus=tb.end_bonus, xdrop=tb.xdrop, diagonal=diag,
+                        window=window, cut=cut, track_cut=tb.flank_min > 0,
+                        bonus_within_cut=tb.end_bonus_cut)
+        else:
+            call.update(kind=0, mode=mode)
+        P.sorted.append(call)
+        return len(P.sorted) - 1
+
+    st = {}  # the sorted call's index, the texts it scores (todo), the unit distances
+    if tb.affine_within is not None and len(uniq) > 1:
+        # `affine_within` (lib.rs:1377-1405): a capped unit-cost pass over the distinct texts
+        # first; only the texts within that many edits of the best get an affine score.
+        w = int(tb.affine_within)
+        at_u = len(P.banded)
+        P.banded.append((rd, tx_all, mode, w, True))
+
+        def stage2():
+            d = P.banded_out[at_u]
+            dmin = min(d)
+            st["unit"] = d
+            st["todo"] = [k for k in range(len(uniq)) if d[k] <= dmin + w]
+            st["at"] = sorted_call([tx_all[k] for k in st["todo"]])
+        P.stage2.append(stage2)
     else:
-        call.update(kind=0, mode=mode)
-    at = len(P.sorted)
-    P.sorted.append(call)
+        st["unit"] = None
+        st["todo"] = list(range(len(uniq)))
+        st["at"] = sorted_call(tx_all)
 
     def fin():
-        xs = P.sorted_out[at]
-        delta = [-xs[rep[i]][0] for i in range(n)]
-        delta_cut = [-xs[rep[i]][1] for i in range(n)]
-        cols = [xs[rep[i]][2] for i in range(n)]
+        xs = P.sorted_out[st["at"]]
+        unit, todo = st["unit"], st["todo"]
+        score, score_cut, cols_k = {}, {}, {}
+        best = None  # (unit distance, affine score), the least distance then the best score
+        for k, (x, xc, cc) in zip(todo, xs):
+            score[k], score_cut[k], cols_k[k] = x, xc, cc
+            du = unit[k] if unit is not None else 0
+            if best is None or (du, -x) < (best[0], -best[1]):
+                best = (du, x)
+        per_edit = tb.affine[0] + tb.affine[1]  # one mismatch per extra edit (lib.rs:1448)
+        delta, delta_cut, cols = [0] * n, [0] * n, [0] * n
+        for i in range(n):
+            k = rep[i]
+            x = score[k] if k in score else best[1] - per_edit * (unit[k] - best[0])
+            delta[i] = -x
+            delta_cut[i] = -score_cut.get(k, x)
+            cols[i] = cols_k.get(k, 0)
         return delta, delta_cut, cols
     return fin
 
@@ -344,16 +386,21 @@ def segmented_batch(ctx, reads: Sequence, txs: Sequence, tb: TieBreak = TieBreak
     [(codes, hits)], hits = [(transcript, [(query start, transcript start, length), ...])]
     with each chain ordered by query start; txs: each transcript's codes.  Returns per read
     (costs per hit, unit) or None when no anchor is shared by every hit.  The DP calls of the
-    whole batch run in one device batch (or through `runner`)."""
+    whole batch run in one device batch -- two with `affine_within` -- (or through
+    `runner`)."""
     P = _Plan()
     tx_arr = [np.ascontiguousarray(np.asarray(t, dtype=np.uint8)) for t in txs]
     fins = [_plan_read(P, tb, np.ascontiguousarray(np.asarray(r, dtype=np.uint8)), hits,
                        tx_arr, hpc) for r, hits in reads]
+    run = runner if runner is not None else gpu_runner(ctx)
+    if P.banded:
+        _, P.banded_out = run([], P.banded)
+    for f in P.stage2:
+        f()
     for c in P.sorted:
         c["sc"] = tb.affine
-    run = runner if runner is not None else gpu_runner(ctx)
-    if P.sorted or P.banded:
-        P.sorted_out, P.banded_out = run(P.sorted, P.banded)
+    if P.sorted:
+        P.sorted_out, _ = run(P.sorted, [])
     return [None if f is None else f() for f in fins]
 
 

@@ -3,8 +3,8 @@ sf_banded_batch for unit costs, per batch): the reference's paper example
 (map/src/lib.rs:3236-3300, costs [-28, -21, -13, -13]) and seeded batches of near-tied
 isoforms -- skipped and inserted segments, other 3' ends, poly(A) tails, leading junk --
 under the default TieBreak and variants of it (flank rule, end bonus cut, diagonal ends,
-unit costs, no tail handling, a wider band), equal read by read to the same host logic with
-its DP on the oracle."""
+unit costs, `affine_within`'s unit-cost prefilter, no tail handling, a wider band), equal
+read by read to the same host logic with its DP on the oracle."""
 import dataclasses
 
 import numpy as np
@@ -39,7 +39,8 @@ def test_paper_example_on_the_device(ctx):
 @pytest.mark.parametrize("variant", [
     {}, {"flank_min": 20}, {"end_bonus_cut": False}, {"end_diagonal": True},
     {"affine": None}, {"tail_trim": False, "tail_bonus": 0}, {"band": 40, "xdrop": 80},
-    {"affine": (1, 4, 6, 2), "end_bonus": 3}])
+    {"affine": (1, 4, 6, 2), "end_bonus": 3}, {"affine_within": 4}, {"affine_within": 0},
+    {"affine_within": 30, "flank_min": 20}])
 def test_batches_equal_the_oracle(ctx, variant):
     from spearfish_gb300 import segmented as G
     tb = dataclasses.replace(G.TieBreak(), **variant)
