@@ -664,9 +664,12 @@ def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, loca
     e2e_once()
     if dist:
         dist.barrier()
+    calls = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        c0 = time.perf_counter()
         e2e_once()
+        calls.append(time.perf_counter() - c0)
     e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / e2e_steps)
     e2e_cells = int(res2["cells"].astype(np.uint64).sum())
     same = all(np.array_equal(res[f], res2[f]) for f in
@@ -676,6 +679,9 @@ def measure_batch(args, cfg, variant, cigar, steps, warmup, dist, ws, rank, loca
     d2h = int(res2.nbytes + used.value * 4)
     e2e = {"value": e2e_cells * ws / e2e_s / 1e9, "unit": "GCUPS", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+           "call_ms_median": statistics.median(calls) * 1e3, "call_ms_min": min(calls) * 1e3,
+           "timing": "value and ms_per_step: the mean over the timed calls; the median and "
+                     "minimum call show host interference on a shared machine",
            "pairs_per_s": len(pairs_list[-1]) * ws / e2e_s,
            "call": "sf_batch_run (C ABI), pinned host pool"}
     plan.close()
@@ -733,7 +739,7 @@ def main():
                     help="c5: texts as windows of a device-resident transcript store (1) or in "
                          "each request's pool (0)")
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload's pairs")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--plain-pairs", type=int, default=200)

@@ -14,9 +14,10 @@
 // single step can add.  The host admits a pass only when its widest row, its scores and this
 // bound fit (sf_plan.cu `fits16`); everything else runs on the 32-bit kernel.
 //
-// Layout.  A field holds value - offset (offset = -0x8000 at row 0), unsigned, so the DPX
-// u16x2 maxima order fields as values, and a - b + 0x7fff7fff has bit 15 (31) set exactly
-// when the low (high) field of a exceeds b's: one IADD3 per pair of traceback decisions.
+// Layout.  A field holds value - offset (offset = -0x8000 at row 0, falling by ext a row, so
+// that F's recurrence is one add-max), unsigned, so the DPX u16x2 maxima order fields as
+// values, and a - b + 0x7fff7fff has bit 15 (31) set exactly when the low (high) field of a
+// exceeds b's: one IADD3 per pair of traceback decisions.
 // Lane l holds band offsets [l*C, l*C + C) as C/2 words: word k = (offset l*C + k,
 // offset l*C + C/2 + k).  Both halves of a word advance together through pass 1, the
 // lane's horizontal-gap chain and pass 2; the warp scan works on per-lane 32-bit values.
@@ -201,23 +202,28 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
   const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;  // + (-ext) mod 2^16
   const uint32_t ext2 = (uint32_t)x.ext * kOne2;
   // Match scores enter as s + mis (mat + mis or 0, so that a plain add of both fields cannot
-  // borrow); the maximum that takes the diagonal subtracts mis again.  A row's table holds
-  // mat + mis in byte p (its pattern base) of ta (low bytes) and tb (high bytes), 0 elsewhere.
-  const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
+  // borrow); the maximum that takes the diagonal adds ext - mis (the row's drift, below, less
+  // mis).  A row's table holds mat + mis in byte p (its pattern base) of ta (low bytes) and tb
+  // (high bytes), 0 elsewhere.
+  const uint32_t dgx2 = ((uint32_t)(x.ext - x.mis) & 0xffffu) * kOne2;  // mod 2^16 a field
   const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
-  const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;  // gt2 against diagonal + mis
+  const uint32_t kGtDg = kGt2 + (uint32_t)(x.mis - x.ext) * kOne2;  // gt2 against that diagonal
   // Products with the opaque -1 issue on the FMA pipe too: a decision a - b + K becomes
   // a * one + (b * mone + K), two IMADs instead of one IADD3 on the ALU pipe, which the
   // maxima, table lookups and pushes keep busier.
   const uint32_t mone = 0u - one;
-  const uint32_t ngo2 = ((uint32_t)(-x.go) & 0xffffu) * kOne2;  // + (-go) mod 2^16
-  const uint32_t kGtGo = kGt2 + go2;                          // gt2 against a value less go
+  const uint32_t fgx2 = ((uint32_t)(x.ext - x.go) & 0xffffu) * kOne2;  // + (ext - go) mod 2^16
+  const uint32_t kGtFo = kGt2 + (uint32_t)(x.go - x.ext) * kOne2;    // gt2 against Hup + ext - go
+  const uint32_t kGtGo = kGt2 + go2;                                  // gt2 against a value less go
   // Warp-scan decays: a lane's gap value falls by ext * C per lane it crosses.  The lane's
   // own chain is the maximum over its cells of H' + ext * k, less go + ext * (C/2 - 1).
   const int32_t dC = x.ext * C, dH = -x.ext * C2;
   const int32_t goX = x.go + x.ext * (C2 - 1);
   const int32_t e_lane = (int32_t)kNeg16 - dC * lane;  // NEG at the band's left end, decayed
-  int32_t off = -(int32_t)kBias16;  // value = field + off
+  // value = field + off, and off falls by ext every row: a row's fields hold its values plus
+  // ext for every row since row 0 (less the rebases), so that F = max(Hup - go, Fup - ext)
+  // is one add-max on fields, F' = max(Hup' + ext - go, Fup'), and the diagonal gains ext.
+  int32_t off = -(int32_t)kBias16;
   uint32_t h[C2], f[C2], sel[C2], smask[kMasks ? C2 : 1];
   int32_t plo, phi;
   g.range(0, plo, phi);
@@ -306,6 +312,7 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
     // align.rs:2462-2468; rows past n + below (empty) never get here.
     const int32_t lo = D1 ? i - g.below : 0, hi = ST ? i + g.above : min(i + g.above, n);
     const int32_t W = ST ? Wc : hi - lo + 1;
+    off -= x.ext;
     if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + (i >> 4));
     const uint32_t pb = 8u * (pw & 3u);
     pw >>= 2;
@@ -329,22 +336,22 @@ __device__ __forceinline__ DRes pair16(const sfk::AffLaunch& a, uint32_t jid, in
 
     // Pass 1: F, H' and the lane's horizontal-gap chain.  F = max(Hup - go, Fup - ext): the
     // 32-bit kernel's floor at NEG only ever lifts values that lose to a reachable one, so
-    // it is left out (F above the band's sentinel sits ext below NEG instead of at it).
+    // it is left out (F from the band's sentinel stays at NEG).
     uint32_t red = 0, pend = 0;  // maximum of H' + ext * k over the lane's words
     uint32_t acc1[G];
 #pragma unroll
     for (int q = 0; q < G; ++q) acc1[q] = 0;
     auto cell = [&](auto kt, uint32_t hd, uint32_t hu, uint32_t fu) {
       constexpr int k = decltype(kt)::value;
-      // F = max(Hup - go, Fup - ext).
-      const uint32_t fj = __viaddmax_u16x2(hu, ngo2, fu * one - ext2);
+      // F = max(Hup - go, Fup - ext), on fields that drift by ext a row.
+      const uint32_t fj = __viaddmax_u16x2(hu, fgx2, fu);
       // This row's column k, after its shift.
       constexpr int sk = (D1 && ROT >= 0) ? (k + ROT + 1) % C2 : k;
       const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[sk]);  // diagonal + s + mis
-      const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
-      // "F extended": fj > Hup - go; "diagonal lost": xx > dgp - mis.
+      const uint32_t xx = __viaddmax_u16x2(dgp, dgx2, fj);
+      // "F extended": fj > Hup + ext - go; "diagonal lost": xx > dgp + ext - mis.
       if constexpr (TB)
-        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtGo),
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtFo),
                                     xx * one + (dgp * mone + kGtDg));
       const uint32_t t = xx * one + ext2 * (uint32_t)k;
       if constexpr (k == 0)
@@ -614,11 +621,12 @@ __device__ __forceinline__ void pair16w(const sfk::AffLaunch& a, uint32_t jid, i
   const uint32_t go2 = (uint32_t)x.go * kOne2;
   const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;
   const uint32_t ext2 = (uint32_t)x.ext * kOne2;
-  const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
+  const uint32_t dgx2 = ((uint32_t)(x.ext - x.mis) & 0xffffu) * kOne2;
   const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
-  const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;
+  const uint32_t kGtDg = kGt2 + (uint32_t)(x.mis - x.ext) * kOne2;
   const uint32_t mone = 0u - one;
-  const uint32_t ngo2 = ((uint32_t)(-x.go) & 0xffffu) * kOne2;
+  const uint32_t fgx2 = ((uint32_t)(x.ext - x.go) & 0xffffu) * kOne2;
+  const uint32_t kGtFo = kGt2 + (uint32_t)(x.go - x.ext) * kOne2;
   const uint32_t kGtGo = kGt2 + go2;
   const int32_t dC = x.ext * C, dH = -x.ext * C2;
   const int32_t goX = x.go + x.ext * (C2 - 1);
@@ -696,6 +704,7 @@ __device__ __forceinline__ void pair16w(const sfk::AffLaunch& a, uint32_t jid, i
     constexpr bool D1 = MODE >= 1, ST = MODE == 2;
     const int32_t lo = D1 ? i - g.below : 0, hi = ST ? i + g.above : min(i + g.above, n);
     const int32_t W = ST ? Wc : hi - lo + 1;
+    off -= x.ext;  // fields drift by ext a row (pair16)
     if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + (i >> 4));
     const uint32_t pb = 8u * (pw & 3u);
     pw >>= 2;
@@ -719,11 +728,11 @@ __device__ __forceinline__ void pair16w(const sfk::AffLaunch& a, uint32_t jid, i
     for (int q = 0; q < G; ++q) acc1[q] = 0;
     auto cell = [&](auto kt, uint32_t hd, uint32_t hu, uint32_t fu) {
       constexpr int k = decltype(kt)::value;
-      const uint32_t fj = __viaddmax_u16x2(hu, ngo2, fu * one - ext2);
+      const uint32_t fj = __viaddmax_u16x2(hu, fgx2, fu);
       const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);
-      const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
+      const uint32_t xx = __viaddmax_u16x2(dgp, dgx2, fj);
       if constexpr (TB)
-        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtGo),
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtFo),
                                     xx * one + (dgp * mone + kGtDg));
       const uint32_t t = xx * one + ext2 * (uint32_t)k;
       if constexpr (k == 0)
@@ -985,11 +994,12 @@ __device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lan
   const uint32_t go2 = (uint32_t)x.go * kOne2;
   const uint32_t next2 = ((uint32_t)(-x.ext) & 0xffffu) * kOne2;
   const uint32_t ext2 = (uint32_t)x.ext * kOne2;
-  const uint32_t nmis2 = ((uint32_t)(-x.mis) & 0xffffu) * kOne2;
+  const uint32_t dgx2 = ((uint32_t)(x.ext - x.mis) & 0xffffu) * kOne2;
   const uint32_t mpm = (uint32_t)(x.mat + x.mis) & 0xffffu;
-  const uint32_t kGtDg = kGt2 + (uint32_t)x.mis * kOne2;
+  const uint32_t kGtDg = kGt2 + (uint32_t)(x.mis - x.ext) * kOne2;
   const uint32_t mone = 0u - one;
-  const uint32_t ngo2 = ((uint32_t)(-x.go) & 0xffffu) * kOne2;
+  const uint32_t fgx2 = ((uint32_t)(x.ext - x.go) & 0xffffu) * kOne2;
+  const uint32_t kGtFo = kGt2 + (uint32_t)(x.go - x.ext) * kOne2;
   const uint32_t kGtGo = kGt2 + go2;
   const int32_t dC = x.ext * C, dH = -x.ext * C2;
   const int32_t goX = x.go + x.ext * (C2 - 1);
@@ -1077,6 +1087,7 @@ __device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lan
     const bool act = fin == 0 && i <= endB;
     const int32_t lo = D1 ? i - g.below : 0, hi = min(i + g.above, n);
     const int32_t W = hi - lo + 1;
+    off -= x.ext;  // fields drift by ext a row (pair16)
     if ((i & 15) == 0) pw = __ldg(a.pool + x.J.p_word + ((i <= m ? i : m) >> 4));
     const uint32_t pb = 8u * (pw & 3u);
     pw >>= 2;
@@ -1131,11 +1142,11 @@ __device__ void pair16h(const sfk::AffLaunch& a, uint32_t jid, bool has, int lan
         hd = D1 ? hk : hdp;
         hdp = hk;
       }
-      const uint32_t fj = __viaddmax_u16x2(hu, ngo2, fu * one - ext2);
+      const uint32_t fj = __viaddmax_u16x2(hu, fgx2, fu);
       const uint32_t dgp = hd * one + __byte_perm(ta, tbl, sel[k]);
-      const uint32_t xx = __viaddmax_u16x2(dgp, nmis2, fj);
+      const uint32_t xx = __viaddmax_u16x2(dgp, dgx2, fj);
       if constexpr (TB)
-        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtGo),
+        acc1[k >> 3] = push2<k & 7>(acc1[k >> 3], fj * one + (hu * mone + kGtFo),
                                     xx * one + (dgp * mone + kGtDg));
       const uint32_t t = xx * one + ext2 * (uint32_t)k;
       if constexpr (k == 0)

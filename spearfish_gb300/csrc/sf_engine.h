@@ -237,7 +237,9 @@ struct sf_context {
   int dev = 0;
   int sms = 0;
   cudaStream_t s = nullptr;
-  static constexpr int kAux = 8;
+  // Auxiliary streams: kMain that buckets share round robin, then kSide for buckets of a
+  // few long passes, so that no other bucket waits behind them.
+  static constexpr int kMain = 8, kSide = 4, kAux = kMain + kSide;
   cudaStream_t aux[kAux] = {};
   cudaEvent_t fork = nullptr, join[kAux] = {};
   std::unique_ptr<sf_plan> cache;  // reused by sf_batch_run
@@ -306,8 +308,8 @@ bool batch_segments_on();
 // far; stage_wait waits for that before it is written again.
 int stage_wait(sf_plan* P);
 int stage_done(sf_plan* P);
-// One execute in parts: the pack and the buckets (bucket u on auxiliary stream
-// (u + soff) mod kAux, also a single bucket with fan_one; `used` collects the streams),
+// One execute in parts: the pack and the buckets (each on its auxiliary stream, the main
+// ones rotated by soff; also a single bucket with fan_one; `used` collects the streams),
 // the auxiliary streams joined back into `s`, then the CIGAR compaction.  plan_launch runs
 // all three; with `evs`, everything runs in order on `s` with an event after each stage.
 int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs, int soff,

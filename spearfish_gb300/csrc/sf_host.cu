@@ -1079,7 +1079,7 @@ int batch_run_segments(sf_context* ctx, int nseg, const uint8_t* pool, uint64_t 
       (void)cudaStreamSynchronize(ctx->tail);
       return fail(rc, msg);
     }
-    soff = (soff + (int)std::max<size_t>(P->buckets.size(), 1)) % sf_context::kAux;
+    soff = (soff + (int)std::max<size_t>(P->buckets.size(), 1)) % sf_context::kMain;
   }
   // Results, segment by segment as their tails end: the records converted while later
   // segments run, the CIGARs copied to the caller after the earlier segments' ones.

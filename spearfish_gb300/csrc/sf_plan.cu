@@ -1018,8 +1018,19 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
   }
   P->wide_warps = wide_warps;
   S.scratch_total = scratch_total;
-  // Streams: round robin over the buckets in launch order, so that their tails overlap.
-  for (size_t u = 0; u < P->buckets.size(); ++u) P->buckets[u].stream = (int)(u % sf_context::kAux);
+  // Streams.  The first buckets (in launch order) of fewer warps than the device has SMs -- a
+  // few long passes: the widest rows, the longest patterns -- take a side stream each, so
+  // that no bucket queues behind their long run; the others go round robin over the main
+  // streams in launch order, so that their tails overlap.  Measured on 100,000 uneven pairs:
+  // 87.5 -> 86.8 ms an execute; every bucket on a stream of its own (16 or 32 streams) took
+  // 106-112 ms, the long passes then starting late among the other kernels' blocks.
+  int nmain = 0, nside = 0;
+  for (auto& b : P->buckets) {
+    if ((int64_t)b.grid * (b.block / 32) < ctx->sms && nside < sf_context::kSide)
+      b.stream = sf_context::kMain + nside++;
+    else
+      b.stream = nmain++ % sf_context::kMain;
+  }
 }
 
 // Device buffers sized for the plan, and its descriptors copied there.
@@ -1219,8 +1230,9 @@ int mark_stage(std::vector<cudaEvent_t>* evs, cudaStream_t s) {
 }
 
 // The first part of an execute: the pack on `s`, then the buckets, fanned out over the
-// auxiliary streams so that their tails overlap (bucket u on stream (u + soff) mod kAux;
-// also a single bucket with `fan_one`).  `used` collects the auxiliary streams launched on.
+// auxiliary streams so that their tails overlap (each bucket on its stream, the main ones
+// rotated by `soff`; also a single bucket with `fan_one`).  `used` collects the auxiliary
+// streams launched on.
 // With `evs`, everything runs in order on `s` with an event after each stage.
 int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* evs, int soff,
                         bool fan_one, bool* used) {
@@ -1251,7 +1263,7 @@ int plan_launch_buckets(sf_plan* P, cudaStream_t s, std::vector<cudaEvent_t>* ev
     const Bucket& b = P->buckets[q];
     cudaStream_t bs = s;
     if (fan) {
-      const int si = (b.stream + soff) % sf_context::kAux;
+      const int si = b.stream < sf_context::kMain ? (b.stream + soff) % sf_context::kMain : b.stream;
       bs = ctx->aux[si];
       if (!mine[si]) CK(cudaStreamWaitEvent(bs, ctx->fork, 0));
       mine[si] = used[si] = true;
