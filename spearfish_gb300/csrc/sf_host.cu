@@ -958,7 +958,7 @@ constexpr uint64_t kSegJobs = 4096;
 // The end of the furthest pool byte the jobs read (patterns, and texts in the pool), at most
 // pool_bytes.
 uint64_t pool_reach(const sf_job_t* jobs, uint64_t count, uint64_t pool_bytes) {
-  constexpr int kT = 8;
+  constexpr int kT = 16;
   uint64_t mx[kT] = {};
   auto end = [&](uint64_t off, uint64_t len) {
     return off >= pool_bytes || len > pool_bytes - off ? pool_bytes : off + len;
@@ -981,7 +981,7 @@ uint64_t pool_reach(const sf_job_t* jobs, uint64_t count, uint64_t pool_bytes) {
 // band cells for affine jobs and matrix cells / 24 for Myers (its cells cost about 1/24 of
 // an affine cell).
 bool batch_even(const sf_job_t* jobs, uint64_t count) {
-  constexpr int kT = 8;
+  constexpr int kT = 16;
   double sum[kT] = {}, mx[kT] = {};
   parallel_chunks(count, 4096, kT, [&](size_t q0, size_t q1, int k) {
     double s = 0, x = 0;

@@ -48,7 +48,7 @@ class HostPool {
  private:
   HostPool() : pid_(getpid()) {
     const unsigned hw = std::thread::hardware_concurrency();
-    const unsigned n = std::min(7u, hw > 1 ? hw - 1 : 0u);
+    const unsigned n = std::min(15u, hw > 1 ? hw - 1 : 0u);
     try {
       for (unsigned k = 0; k < n; ++k) threads_.emplace_back([this] { loop(); });
     } catch (...) {

@@ -334,7 +334,7 @@ int build_sequences(sf_plan* P, BuildScratch& S) {
     off = (u & 1) ? p.t_off : p.p_off;
     len = (u & 1) ? p.n : p.m;
   };
-  constexpr int kChunks = 8;
+  constexpr int kChunks = 16;
   bool in_order = true;
   // Per chunk of passes (the same chunks below): its new sequences and their words, counted
   // as if the pool were in order (a sequence equal to the one before it shares its words).
@@ -540,7 +540,7 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
   // Slots in each kind's arrays, in pass order: each chunk's Myers passes counted, then the
   // slots written.  Myers classes are checked here, so that the parallel part below cannot
   // fail.
-  constexpr int kT = 8;
+  constexpr int kT = 16;
   uint64_t nmy[kT + 1] = {}, bad[kT];
   for (int k = 0; k < kT; ++k) bad[k] = UINT64_MAX;
   parallel_chunks(np, 4096, kT, [&](size_t q0, size_t q1, int k) {
@@ -589,7 +589,7 @@ int describe_passes(sf_plan* P, BuildScratch& S, bool use16) {
   ops_need.resize(n_affine);
   per.resize(np);
   has_item.resize(np);
-  constexpr int kMaxThreads = 8;
+  constexpr int kMaxThreads = 16;
   uint64_t scratch_max[kMaxThreads] = {};
   bool kcut[kMaxThreads] = {};
   // Descriptors of passes [q0, q1), each written at its slot.
@@ -701,7 +701,7 @@ void lay_out_outputs(sf_plan* P, BuildScratch& S) {
   auto& wlist = S.wlist;
   auto& items = S.items;
   // Two passes over the same chunks: each chunk's totals, then its entries at their places.
-  constexpr int kT = 8;
+  constexpr int kT = 16;
   struct Sums {
     uint64_t tb = 0, ops = 0, walks = 0;
   } sum[kT + 1];
@@ -805,7 +805,7 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
   const sf_context* ctx = P->ctx;
   const auto& items = S.items;
   const size_t ni = items.size();
-  constexpr int kT = 8;
+  constexpr int kT = 16;
   // Buckets in key order; within a bucket, longest work first (ties in job order).
   // Each item's bucket first: keys pack into 15-bit codes ordered as the keys are (kind < 8,
   // C < 128, lanes a power of two up to 64, coded by its log2), so a bit set of the codes
@@ -914,15 +914,16 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
     b.work = bwork[u];
   }
   // Longest first within a bucket, by work rounded to 1/16 of its power of two (a stable
-  // counting sort: equal rounded work keeps job order).  Buckets of many items sort on the
-  // host pool one at a time; the others sort side by side.
+  // counting sort: equal rounded work keeps job order).  A bucket of a quarter of the items
+  // or more sorts on the host pool by itself; the others sort side by side, one thread to a
+  // bucket (config 3's 22 buckets: 1.6 -> 0.8 ms, against three pool dispatches a bucket).
   auto wbin = [](uint64_t w) -> uint32_t {
     if (w < 16) return (uint32_t)w;
     const int e = 63 - __builtin_clzll(w);  // w in [2^e, 2^(e+1))
     return (uint32_t)(16 * (e - 3) + ((w >> (e - 4)) & 15));
   };
   constexpr uint32_t kBins = 16 * 61 + 16;
-  constexpr size_t kBig = 4096;
+  const size_t kBig = std::max<size_t>(4096, ni / 4);
   auto& tmp = S.byb_tmp;
   std::vector<uint64_t> bin_at((size_t)kT * kBins);
   for (size_t u = 0; u < nb; ++u) {
@@ -1502,7 +1503,7 @@ int jobs_to_passes(const sf_job_t* jobs, uint64_t count, const sf_affine_t* scor
   ps.resize(count);
   // Chunks in parallel; each stops at its first bad job, and the first bad job of all is
   // converted again here, so that its error is the calling thread's.
-  constexpr int kMaxThreads = 8;
+  constexpr int kMaxThreads = 16;
   uint64_t first_bad[kMaxThreads];
   for (int w = 0; w < kMaxThreads; ++w) first_bad[w] = UINT64_MAX;
   parallel_chunks(count, 2048, kMaxThreads, [&](size_t q0, size_t q1, int w) {
@@ -1537,7 +1538,7 @@ int plan_results(sf_plan* P, sf_result_t* results, uint32_t* ops, uint64_t ops_c
   const size_t np = P->passes.size();
   // Compacted op order = walk-list order = pass order among CIGAR passes: each chunk's ops
   // counted while its results convert, then its passes' offsets.
-  constexpr int kT = 8;
+  constexpr int kT = 16;
   uint64_t ops_of[kT + 1] = {};
   auto has_ops = [](const Pass& p) {
     return p.want_cigar && p.kind != PK_LOCAL && p.kind != PK_MYERS;
