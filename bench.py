@@ -76,8 +76,8 @@ def workload_name(cfg, variant="base", cigar=True) -> str:
 
 OPS_PER_CELL = {"affine_tb": 12, "affine": 10, "myers": 0.625}
 # sf_int_peak counts 3 int32 ops per chain step; ncu counts 2.094 instructions per step (an
-# IMAD on the FMA pipe and a fused add-max on the ALU pipe, the loop included), so its rate
-# in instructions is Tops x 2.094 / 3 (profiles/int_peak.md).
+# IMAD on the FMA pipe and a fused add-max on the ALU pipe, the loop included; one capture of
+# the probe kernel alone), so its rate in instructions is Tops x 2.094 / 3.
 INT_PEAK_INSTR_PER_STEP = 2.094
 
 
