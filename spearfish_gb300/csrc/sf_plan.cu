@@ -923,12 +923,12 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
     return (uint32_t)(16 * (e - 3) + ((w >> (e - 4)) & 15));
   };
   constexpr uint32_t kBins = 16 * 61 + 16;
-  const size_t kBig = std::max<size_t>(4096, ni / 4);
+  const size_t big = std::max<size_t>(4096, ni / 4);
   auto& tmp = S.byb_tmp;
   std::vector<uint64_t> bin_at((size_t)kT * kBins);
   for (size_t u = 0; u < nb; ++u) {
     Bucket& b = P->buckets[u];
-    if (b.count < kBig) continue;
+    if (b.count < big) continue;
     const auto* src = byb.data() + b.first;
     const size_t n = b.count;
     std::fill(bin_at.begin(), bin_at.end(), 0);
@@ -974,7 +974,7 @@ void build_buckets(sf_plan* P, BuildScratch& S) {
     std::vector<std::pair<uint64_t, uint32_t>> part;
     for (size_t u = u0; u < u1; ++u) {
       Bucket& b = P->buckets[u];
-      if (b.count >= kBig) continue;
+      if (b.count >= big) continue;
       auto b0 = byb.begin() + (ptrdiff_t)b.first, b1 = b0 + (ptrdiff_t)b.count;
       std::fill(bin_n.begin(), bin_n.end(), 0u);
       for (auto it = b0; it != b1; ++it) bin_n[kBins - 1 - wbin(it->first) + 1]++;
