@@ -1,10 +1,50 @@
 // Byte codes -> 2-bit packed sequences in HBM, and the compaction of CIGAR ops.
 //
 // Packing is HBM-bound byte work: one warp per sequence, each lane building whole 16-base
-// words from 16 consecutive bytes (coalesced 512-byte spans per warp), written once.
+// words from 16 consecutive bytes (two aligned 16-byte loads inside the sequence, coalesced
+// 512-byte spans per warp), written once.
 #include "sf_internal.cuh"
 
 namespace {
+
+// Four byte codes (their low two bits) -> one byte, code b at bits 2b: the multiply moves byte
+// b's bits 8b..8b+1 to 24 + 2b, and the other products land below bit 24 in fields that do not
+// overlap, so nothing carries into the top byte.
+__device__ __forceinline__ uint32_t pack4(uint32_t u) {
+  return ((u & 0x03030303u) * 0x01041040u) >> 24;
+}
+
+// Word w of a sequence read forwards: bases 16w .. 16w + 15, base x at byte x - 1 (base 0, the
+// pad, reads as 0).  Every word's first byte sits at the same offset in its 16-byte line, sh =
+// 4Q + r8 / 8 (uniform for the sequence, so Q is a template argument).  Words whose two lines
+// lie inside the sequence's bytes take two 16-byte loads and four funnel shifts; the first
+// word and the words at the sequence's end take byte loads.  No load leaves the sequence.
+template <int Q>
+__device__ __forceinline__ void pack_forward(uint32_t* dst, const uint8_t* src, uint64_t len,
+                                             uint64_t words, int lane, uint32_t r8) {
+  const uint64_t s0 = (uint64_t)(uintptr_t)src;
+  for (uint64_t w = lane; w < words; w += 32) {
+    const uint64_t a0 = s0 + 16 * w - 1;
+    const uint64_t al = a0 & ~uint64_t(15);
+    uint32_t v = 0;
+    if (w > 0 && al >= s0 && al + 32 <= s0 + len) {
+      const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(al));
+      const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(al + 16));
+      const uint32_t x[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      v = pack4(__funnelshift_r(x[Q], x[Q + 1], r8)) |
+          pack4(__funnelshift_r(x[Q + 1], x[Q + 2], r8)) << 8 |
+          pack4(__funnelshift_r(x[Q + 2], x[Q + 3], r8)) << 16 |
+          pack4(__funnelshift_r(x[Q + 3], x[Q + 4], r8)) << 24;
+    } else {
+#pragma unroll
+      for (int b = 0; b < 16; ++b) {
+        const uint64_t pos = 16 * w + b;
+        if (pos >= 1 && pos - 1 < len) v |= (uint32_t)(src[pos - 1] & 3) << (2 * b);
+      }
+    }
+    dst[w] = v;
+  }
+}
 
 __global__ void __launch_bounds__(256) pack_kernel(sfk::PackLaunch a) {
   const int lane = threadIdx.x & 31;
@@ -48,13 +88,23 @@ __global__ void __launch_bounds__(256) pack_kernel(sfk::PackLaunch a) {
       continue;
     }
     const uint8_t* src = a.bytes + (off & ~(uint64_t(3) << 62));
+    if (!rev) {
+      const uint32_t sh = (uint32_t)(((uint64_t)(uintptr_t)src + 15) & 15);  // (src - 1) mod 16
+      const uint32_t r8 = 8 * (sh & 3);
+      switch (sh >> 2) {
+        case 0: pack_forward<0>(dst, src, len, words, lane, r8); break;
+        case 1: pack_forward<1>(dst, src, len, words, lane, r8); break;
+        case 2: pack_forward<2>(dst, src, len, words, lane, r8); break;
+        default: pack_forward<3>(dst, src, len, words, lane, r8); break;
+      }
+      continue;
+    }
     for (uint64_t w = lane; w < words; w += 32) {
       uint32_t v = 0;
 #pragma unroll
       for (int b = 0; b < 16; ++b) {
         const uint64_t pos = 16 * w + b;
-        if (pos >= 1 && pos - 1 < len)
-          v |= (uint32_t)(src[rev ? len - pos : pos - 1] & 3) << (2 * b);
+        if (pos >= 1 && pos - 1 < len) v |= (uint32_t)(src[len - pos] & 3) << (2 * b);
       }
       dst[w] = v;
     }
